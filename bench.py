@@ -1,0 +1,450 @@
+"""SpMV throughput benchmark (GB/s of algorithmic bytes, % of HBM peak).
+
+Default workload: FP64 CSR SpMV on the power-law matrix (N = 2,000,000,
+lognormal(2.0, 1.2) row lengths clipped to [1, 4096], uniform distinct
+columns, N(0,1) values, int32 indices; seeded synthetic data).  One step = one
+y = A*x over the whole matrix.  The 0.4 GB working set is larger than L2, so no
+flush is needed between steps.
+
+    python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+                    [--workload power_law|stencil27|laplacian] [--format csr|coo|dia|ell|hyb|hdc]
+                    [--dtype f64|f32] [--suite]
+
+Under torchrun (N > 1) every rank runs an independent replica (rows of
+different matrices are independent objects; no collective on the data path),
+`value` is the sum over ranks and `scaling` is "weak".
+
+--impl reference times the reference's CPU algorithm for the same workload:
+the oracle's restatement of Morpheus's OpenMP multiply
+(impl/Csr/OpenMP/Morpheus_Multiply_Impl.hpp:37-58), on all host cores, rank 0
+only (the reference library itself needs Kokkos and cannot be built here).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+FALLBACK_HBM_GBS = 6800.0
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+# --------------------------------------------------------------------------
+# workloads
+# --------------------------------------------------------------------------
+
+def build_workload(name: str, fmt: str, dtype, seed: int):
+    from morpheus_gb300 import generators as gen
+    if name == "power_law":
+        A = gen.power_law(2_000_000, seed=seed, dtype=dtype)
+    elif name == "stencil27":
+        A = gen.stencil_27pt(160, seed=seed, dtype=dtype)
+        if fmt == "hdc":
+            A = gen.add_offband(A, 0.01, seed=seed + 1)
+    elif name == "laplacian":
+        A = gen.laplacian_2d(256, dtype=dtype)
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    if fmt == "csr":
+        hm = A
+    elif fmt == "coo":
+        hm = gen.csr_to_coo_host(A)
+    elif fmt == "dia":
+        hm = gen.csr_to_dia_host(A)
+    elif fmt == "ell":
+        p90 = int(np.percentile(np.diff(A["row_offsets"]), 90))
+        hm = gen.csr_to_hyb_host(A, p90)["ell"] if name == "power_law" else gen.csr_to_ell_host(A)
+        if name == "power_law":  # ELL part only: rows longer than p90 are truncated -> use HYB for full
+            raise SystemExit("power-law ELL at the p90 width needs the COO remainder: use --format hyb")
+    elif fmt == "hyb":
+        p90 = int(np.percentile(np.diff(A["row_offsets"]), 90))
+        hm = gen.csr_to_hyb_host(A, p90 if name == "power_law" else max(1, A["nnz"] // A["nrows"]))
+    elif fmt == "hdc":
+        hm = gen.csr_to_hdc_host(A)
+    else:
+        raise SystemExit(f"unknown format {fmt}")
+    return A, hm
+
+
+def algorithmic_bytes(hm: dict, vbytes: int) -> int:
+    """Bytes one SpMV must move: every stored index/value once, x once, y once."""
+    f = hm["format"]
+    n, m = hm["nrows"], hm["ncols"]
+    xy = (m + n) * vbytes
+    if f == 0:
+        return hm["nnz"] * (8 + vbytes) + xy
+    if f == 1:
+        return hm["nnz"] * (4 + vbytes) + 4 * (n + 1) + xy
+    if f == 2:
+        return hm["ndiags"] * n * vbytes + 4 * hm["ndiags"] + xy
+    if f == 3:
+        return n * hm["width"] * (4 + vbytes) + xy
+    if f == 4:
+        e, c = hm["ell"], hm["coo"]
+        return n * e["width"] * (4 + vbytes) + c["nnz"] * (8 + vbytes) + xy
+    if f == 5:
+        d, c = hm["dia"], hm["csr"]
+        return d["ndiags"] * n * vbytes + 4 * d["ndiags"] + c["nnz"] * (4 + vbytes) + 4 * (n + 1) + xy
+    raise ValueError(f)
+
+
+def host_arrays(hm: dict):
+    out = []
+    for k, v in hm.items():
+        if isinstance(v, dict):
+            out += host_arrays(v)
+        elif isinstance(v, np.ndarray):
+            out.append((k, v))
+    return out
+
+
+# --------------------------------------------------------------------------
+# clocks
+# --------------------------------------------------------------------------
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        time.sleep(0.15)
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        rows = [r.split(",") for r in out.strip().splitlines() if r.count(",") >= 8]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if "Active" in r[5 + i]
+                          and "Not" not in r[5 + i]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# --------------------------------------------------------------------------
+# CPU baseline (oracle restatement of the reference OpenMP multiply)
+# --------------------------------------------------------------------------
+
+def cpu_multiply_timing(hm: dict, x: np.ndarray, budget_s: float, threads: int, min_reps: int = 3):
+    from oracle import oracle as O
+    from oracle.build import build_oracle
+    build_oracle()
+    om = O.OracleMatrix.from_host(hm)
+    y = np.zeros(hm["nrows"], dtype=x.dtype)
+    om.multiply(x, y, init=True, threads=threads)  # warm
+    times = []
+    t_end = time.perf_counter() + budget_s
+    while len(times) < min_reps or time.perf_counter() < t_end:
+        t0 = time.perf_counter()
+        om.multiply(x, y, init=True, threads=threads)
+        times.append(time.perf_counter() - t0)
+        if len(times) >= 10000:
+            break
+    return times
+
+
+def run_reference(args, rank: int):
+    if rank != 0:
+        return
+    dtype = np.float64 if args.dtype == "f64" else np.float32
+    A, hm = build_workload(args.workload, args.format, dtype, seed=0)
+    vbytes = np.dtype(dtype).itemsize
+    nbytes = algorithmic_bytes(hm, vbytes)
+    x = np.random.default_rng(1).uniform(-1, 1, hm["ncols"]).astype(dtype)
+    from oracle import oracle as O
+    from oracle.build import build_oracle
+    build_oracle()
+    threads = O.max_threads()
+    om = O.OracleMatrix.from_host(hm)
+    y = np.zeros(hm["nrows"], dtype=dtype)
+    for _ in range(args.warmup):
+        om.multiply(x, y, init=True, threads=threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        om.multiply(x, y, init=True, threads=threads)
+    el = time.perf_counter() - t0
+    gbs = nbytes * args.steps / el / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": gbs, "unit": "GB/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": args.dtype,
+        "data": "synthetic (seeded)", "config": config_dict(args, hm),
+        "cpu_baseline": {"value": gbs, "unit": "GB/s", "cores": threads, "kind": "port",
+                         "sample": f"full matrix, {args.steps} timed multiplies (reference OpenMP "
+                                   f"algorithm restated in oracle/oracle.cpp)"},
+        "e2e": {"value": gbs, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+METRIC = "SpMV GB/s (% HBM peak)"
+
+
+def config_dict(args, hm):
+    return {"workload": f"{args.workload}_{args.format}_{args.dtype}", "format": args.format.upper(),
+            "nrows": hm["nrows"], "ncols": hm["ncols"], "nnz": hm["nnz"],
+            "l2": "inputs larger than L2 (no flush needed)" if args.workload != "laplacian"
+            else "L2 flushed between steps (256 MB scratch write)",
+            "parallelism": f"replicas x{args.gpus}"}
+
+
+# --------------------------------------------------------------------------
+# GPU arm
+# --------------------------------------------------------------------------
+
+def run_gpu(args, rank: int, world: int, local_rank: int):
+    import ctypes as C
+
+    import torch
+
+    import morpheus_gb300 as mgb
+    from morpheus_gb300 import _lib
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    dtype = np.float64 if args.dtype == "f64" else np.float32
+    tdtype = torch.float64 if args.dtype == "f64" else torch.float32
+    vbytes = np.dtype(dtype).itemsize
+    A, hm = build_workload(args.workload, args.format, dtype, seed=rank)
+    nbytes = algorithmic_bytes(hm, vbytes)
+    M = mgb.matrix_from_host(hm, device=dev)
+    x_np = np.random.default_rng(1 + rank).uniform(-1, 1, hm["ncols"]).astype(dtype)
+    x = torch.from_numpy(x_np).to(dev)
+    y = torch.zeros(hm["nrows"], dtype=tdtype, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    flush = None
+    if args.workload == "laplacian":  # L2-resident: flush with a >L2 write between steps
+        flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    # correctness gate on this exact input (rank 0): GPU vs oracle OpenMP multiply
+    check_err = None
+    if rank == 0 and not args.skip_check:
+        from oracle import oracle as O
+        from oracle.build import build_oracle
+        build_oracle()
+        ref = O.OracleMatrix.from_host(hm).multiply(x_np, threads=O.max_threads())
+        mgb.multiply(M, x, y, init=True)
+        torch.cuda.synchronize()
+        yy = y.cpu().numpy().astype(np.float64)
+        check_err = float(np.linalg.norm(yy - ref) / max(np.linalg.norm(ref), 1e-300))
+
+    for _ in range(args.warmup):
+        mgb.multiply(M, x, y, init=True)
+    torch.cuda.synchronize()
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    time.sleep(0.3)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    per = []
+    torch.cuda.synchronize()
+    if flush is None:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            mgb.multiply(M, x, y, init=True)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1)
+        kernel_ms = ms / args.steps
+    else:
+        # flush between steps; time each SpMV separately with events
+        ms = 0.0
+        for _ in range(args.steps):
+            flush.fill_(1)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            mgb.multiply(M, x, y, init=True)
+            b.record(stream)
+            per.append((a, b))
+        torch.cuda.synchronize()
+        times = [a.elapsed_time(b) for a, b in per]
+        ms = sum(times)
+        kernel_ms = ms / args.steps
+    clocks = sampler.stop()
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        kernel_ms = ms / args.steps
+    value = world * nbytes * args.steps / (ms * 1e-3) / 1e9
+
+    # e2e: host buffers through the C ABI, H2D of the step's inputs and D2H of y inside the region
+    pinned = {}
+    h2d = 0
+    for k, arr in host_arrays(hm):
+        t = torch.from_numpy(np.ascontiguousarray(arr)).pin_memory()
+        pinned[id(arr)] = t
+        h2d += t.numel() * t.element_size()
+    xh = torch.from_numpy(x_np).pin_memory()
+    h2d += xh.numel() * xh.element_size()
+    yh = torch.empty(hm["nrows"], dtype=tdtype).pin_memory()
+    d2h = yh.numel() * yh.element_size()
+    dev_bufs = mgb.matrix_from_host(hm, device=dev)  # destination buffers of the copies
+
+    def dev_tensors(Mx):
+        out = []
+        for name in ("_ri", "_ro", "_ci", "_off", "_v"):
+            if hasattr(Mx, name):
+                out.append(getattr(Mx, name))
+        for sub in ("_ell", "_coo", "_dia", "_csr"):
+            if hasattr(Mx, sub):
+                out += dev_tensors(getattr(Mx, sub))
+        return out
+
+    host_list = [pinned[id(a)] for _, a in host_arrays(hm)]
+    dst_list = dev_tensors(dev_bufs)
+    # pair host and device tensors by size and dtype (same traversal order)
+    pairs = []
+    used = set()
+    for h in host_list:
+        for i, d in enumerate(dst_list):
+            if i not in used and d.numel() == h.numel() and d.dtype == h.dtype:
+                pairs.append((h, d))
+                used.add(i)
+                break
+    e2e_steps = max(1, min(args.steps, args.e2e_steps))
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        for h, d in pairs:
+            d.copy_(h, non_blocking=True)
+        x.copy_(xh, non_blocking=True)
+        mgb.multiply(dev_bufs, x, y, init=True)
+        yh.copy_(y, non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / e2e_steps
+    e2e_val = world * nbytes / (e2e_ms * 1e-3) / 1e9
+
+    if rank != 0:
+        return
+    peak, peak_src = peaks()
+    achieved = nbytes / (kernel_ms * 1e-3) / 1e9
+    traffic = profile_traffic(args)
+    line = {
+        "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": args.dtype,
+        "data": "synthetic (seeded power-law / stencil generators, N(0,1) values)",
+        "config": config_dict(args, hm),
+        "pct_hbm_peak": 100.0 * achieved / peak,
+        "rel_err_vs_oracle": check_err,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured"
+                     else "fallback 6.8 TB/s", "algorithmic_bytes_per_launch": nbytes},
+        "e2e": {"value": e2e_val, "unit": "GB/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": e2e_ms},
+        "gpu_launches": args.steps * launches_per_step(hm),
+        "clocks": clocks,
+    }
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        from oracle import oracle as O
+        threads = O.max_threads()
+        times = cpu_multiply_timing(hm, x_np, args.cpu_budget, threads)
+        med = statistics.median(times)
+        line["cpu_baseline"] = {"value": nbytes / med / 1e9, "unit": "GB/s", "cores": threads, "kind": "port",
+                                "sample": f"full matrix, {len(times)} multiplies over ~{args.cpu_budget:.0f} s, "
+                                          "median (reference OpenMP algorithm restated in oracle/oracle.cpp)"}
+    print(json.dumps(line), flush=True)
+
+
+def launches_per_step(hm) -> int:
+    f = hm["format"]
+    if f == 0:
+        return 2  # chunk kernel + carry fix-up
+    if f == 4:
+        return 1 + (2 if hm["coo"]["nnz"] else 0)
+    return 1
+
+
+def profile_traffic(args):
+    """DRAM bytes per launch from the committed ncu summary, if one exists."""
+    p = os.path.join(ROOT, "profiles", f"spmv_{args.format}_{args.workload}_{args.dtype}.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("dram_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip().split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="mgb", choices=["mgb", "reference"])
+    ap.add_argument("--workload", default="power_law", choices=["power_law", "stencil27", "laplacian"])
+    ap.add_argument("--format", default="csr", choices=["csr", "coo", "dia", "ell", "hyb", "hdc"])
+    ap.add_argument("--dtype", default="f64", choices=["f64", "f32"])
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--cpu-budget", type=float, default=10.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--skip-check", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    try:
+        run_gpu(args, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,176 @@
+/*
+ * mgb.h -- C ABI of morpheus-gb300, a GB300 (sm_103a) implementation of the
+ * Morpheus sparse matrix-vector hot path.
+ *
+ * Every entry point takes non-owning DEVICE pointers plus sizes and a CUDA
+ * stream (NULL = the legacy default stream), returns an mgb_status, never
+ * exits and never throws.  SpMV and waxpby are asynchronous on the stream;
+ * the scalar-returning dot/reduce synchronise the stream before returning,
+ * like the reference's CUDA dot/reduce (which copy the scalar back).
+ *
+ * Each declaration names the reference interface it replaces (paths relative
+ * to the Morpheus project root).  The reference is a C++ template library, so
+ * "replaces" means: the body of the Cuda-space overload that
+ * Morpheus::multiply / convert / dot / reduce / waxpby dispatch to for that
+ * container.  The C++ front end in Morpheus_GB300.hpp keeps the reference's
+ * template signatures and calls these functions.
+ */
+#ifndef MGB_H
+#define MGB_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes: one per reference exception class
+ * (core/src/Morpheus_Exceptions.hpp:32-73) plus CUDA / timeout / argument. */
+typedef enum mgb_status {
+  MGB_SUCCESS                 = 0,
+  MGB_ERR_NOT_IMPLEMENTED     = 1, /* NotImplementedException   */
+  MGB_ERR_FORMAT_CONVERSION   = 2, /* FormatConversionException */
+  MGB_ERR_INVALID_INPUT       = 3, /* InvalidInputException     */
+  MGB_ERR_RUNTIME             = 4, /* RuntimeException          */
+  MGB_ERR_IO                  = 5, /* IOException               */
+  MGB_ERR_CUDA                = 6, /* a CUDA runtime call failed */
+  MGB_ERR_TIMEOUT             = 7, /* a bounded device wait ran out */
+  MGB_ERR_BAD_ARGUMENT        = 8, /* null pointer / negative size / bad enum */
+  MGB_ERR_ALLOC               = 9  /* device allocation failed  */
+} mgb_status;
+
+/* Format enum, same order as Morpheus::formats_e
+ * (core/src/Morpheus_FormatsRegistry.hpp:56-64). */
+typedef enum mgb_format {
+  MGB_COO_FORMAT = 0,
+  MGB_CSR_FORMAT = 1,
+  MGB_DIA_FORMAT = 2,
+  MGB_ELL_FORMAT = 3,
+  MGB_HYB_FORMAT = 4,
+  MGB_HDC_FORMAT = 5,
+  MGB_NFORMATS   = 6
+} mgb_format;
+
+/* ELL padding marker (core/src/Morpheus_EllMatrix.hpp:563). */
+#define MGB_INVALID_INDEX (-1)
+
+/* ---- container descriptors (device pointers, column-major slabs) -------- */
+
+/* core/src/Morpheus_CooMatrix.hpp: row_indices/column_indices/values[nnz] */
+typedef struct mgb_coo {
+  int64_t nrows, ncols, nnz;
+  int32_t* row_indices;
+  int32_t* column_indices;
+  void* values; /* double* or float* per the entry point's suffix */
+} mgb_coo;
+
+/* core/src/Morpheus_CsrMatrix.hpp:533-537 */
+typedef struct mgb_csr {
+  int64_t nrows, ncols, nnz;
+  int32_t* row_offsets; /* nrows + 1 */
+  int32_t* column_indices;
+  void* values;
+} mgb_csr;
+
+/* core/src/Morpheus_DiaMatrix.hpp:192-201.  values(i, n) is at
+ * values[i + pitch * n]; pitch = pad(nrows, 32) (the reference's
+ * get_pad_size, core/src/impl/Dia/Morpheus_Utils_Impl.hpp:33-36). */
+typedef struct mgb_dia {
+  int64_t nrows, ncols, nnz, ndiags, pitch;
+  int32_t* diagonal_offsets; /* ndiags, ascending */
+  void* values;              /* pitch * ndiags */
+} mgb_dia;
+
+/* core/src/Morpheus_EllMatrix.hpp:189-202.  Slot (i, n) is at
+ * [i + pitch * n] for n < width; width = pad(entries_per_row, 32);
+ * pitch = nrows.  Padding slots hold (MGB_INVALID_INDEX, 0). */
+typedef struct mgb_ell {
+  int64_t nrows, ncols, nnz, entries_per_row, width, pitch;
+  int32_t* column_indices;
+  void* values;
+} mgb_ell;
+
+/* core/src/Morpheus_HybMatrix.hpp:473-476: ELL part + COO remainder. */
+typedef struct mgb_hyb {
+  mgb_ell ell;
+  mgb_coo coo;
+} mgb_hyb;
+
+/* core/src/Morpheus_HdcMatrix.hpp:464-467: DIA part + CSR remainder. */
+typedef struct mgb_hdc {
+  mgb_dia dia;
+  mgb_csr csr;
+} mgb_hdc;
+
+/* ---- library ----------------------------------------------------------- */
+
+/* Human-readable name of a status code (static storage). */
+const char* mgb_status_string(int status);
+
+/* Library version as major*10000 + minor*100 + patch. */
+int mgb_version(void);
+
+/* Text of the last CUDA error seen by this thread (static storage). */
+const char* mgb_last_cuda_error_string(void);
+
+/* ---- SpMV: y = A*x (init != 0) or y += A*x (init == 0) ------------------
+ * Morpheus::multiply<ExecSpace>(A, x, y[, init])
+ * (core/src/Morpheus_Multiply.hpp:57-78).  x has ncols entries, y nrows. */
+
+/* replaces impl/Csr/Cuda/Morpheus_Multiply_Impl.hpp:50-157 */
+int mgb_spmv_csr_f64(const mgb_csr* A, const double* x, double* y, int init, void* stream);
+int mgb_spmv_csr_f32(const mgb_csr* A, const float* x, float* y, int init, void* stream);
+
+/* replaces impl/Coo/Cuda/Morpheus_Multiply_Impl.hpp:50-176.  Like the
+ * reference's CUDA path, A must be sorted by row (columns in any order). */
+int mgb_spmv_coo_f64(const mgb_coo* A, const double* x, double* y, int init, void* stream);
+int mgb_spmv_coo_f32(const mgb_coo* A, const float* x, float* y, int init, void* stream);
+
+/* replaces impl/Dia/Cuda/Morpheus_Multiply_Impl.hpp:41-85 */
+int mgb_spmv_dia_f64(const mgb_dia* A, const double* x, double* y, int init, void* stream);
+int mgb_spmv_dia_f32(const mgb_dia* A, const float* x, float* y, int init, void* stream);
+
+/* replaces impl/Ell/Cuda/Morpheus_Multiply_Impl.hpp:41-80 */
+int mgb_spmv_ell_f64(const mgb_ell* A, const double* x, double* y, int init, void* stream);
+int mgb_spmv_ell_f32(const mgb_ell* A, const float* x, float* y, int init, void* stream);
+
+/* replaces impl/Hyb/Cuda/Morpheus_Multiply_Impl.hpp:42-53 (ELL init, then COO
+ * accumulate); the COO part must be sorted by row. */
+int mgb_spmv_hyb_f64(const mgb_hyb* A, const double* x, double* y, int init, void* stream);
+int mgb_spmv_hyb_f32(const mgb_hyb* A, const float* x, float* y, int init, void* stream);
+
+/* replaces impl/Hdc/Cuda/Morpheus_Multiply_Impl.hpp:42-53 (DIA init, then CSR
+ * accumulate), fused into one pass over the rows. */
+int mgb_spmv_hdc_f64(const mgb_hdc* A, const double* x, double* y, int init, void* stream);
+int mgb_spmv_hdc_f32(const mgb_hdc* A, const float* x, float* y, int init, void* stream);
+
+/* ---- dense vector ops ---------------------------------------------------- */
+
+/* Morpheus::dot<ExecSpace>(n, x, y) (core/src/Morpheus_Dot.hpp:50-58);
+ * replaces impl/DenseVector/Cuda/Morpheus_Dot_Impl.hpp:59-144.
+ * Writes the scalar to *result (host) and synchronises the stream. */
+int mgb_dot_f64(int64_t n, const double* x, const double* y, double* result, void* stream);
+int mgb_dot_f32(int64_t n, const float* x, const float* y, float* result, void* stream);
+
+/* Asynchronous dot: the scalar is written to device memory d_result. */
+int mgb_dot_f64_async(int64_t n, const double* x, const double* y, double* d_result, void* stream);
+int mgb_dot_f32_async(int64_t n, const float* x, const float* y, float* d_result, void* stream);
+
+/* Morpheus::reduce<ExecSpace>(in, size) (core/src/Morpheus_Reduction.hpp:46-52);
+ * replaces impl/DenseVector/Cuda/Morpheus_Reduction_Impl.hpp:175-234. */
+int mgb_reduce_f64(const double* in, int64_t size, double* result, void* stream);
+int mgb_reduce_f32(const float* in, int64_t size, float* result, void* stream);
+int mgb_reduce_f64_async(const double* in, int64_t size, double* d_result, void* stream);
+int mgb_reduce_f32_async(const float* in, int64_t size, float* d_result, void* stream);
+
+/* Morpheus::waxpby<ExecSpace>(n, alpha, x, beta, y, w): w = alpha*x + beta*y
+ * (core/src/Morpheus_WAXPBY.hpp:52-64); replaces
+ * impl/DenseVector/Cuda/Morpheus_WAXPBY_Impl.hpp:40-70. */
+int mgb_waxpby_f64(int64_t n, double alpha, const double* x, double beta, const double* y, double* w, void* stream);
+int mgb_waxpby_f32(int64_t n, float alpha, const float* x, float beta, const float* y, float* w, void* stream);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* MGB_H */

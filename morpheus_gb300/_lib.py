@@ -1,0 +1,100 @@
+"""ctypes binding of libmorpheus_gb300.so (the C ABI declared in include/mgb.h).
+
+The library is built in-tree by morpheus_gb300.build.  There is no CPU
+fallback: if the shared object is missing or cannot be loaded, every compute
+call raises instead of silently running elsewhere.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+from .exceptions import raise_for_status
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmorpheus_gb300.so")
+
+_lock = threading.Lock()
+_lib = None
+
+i64 = C.c_int64
+i32p = C.POINTER(C.c_int32)
+vp = C.c_void_p
+
+
+class Coo(C.Structure):
+    _fields_ = [("nrows", i64), ("ncols", i64), ("nnz", i64),
+                ("row_indices", vp), ("column_indices", vp), ("values", vp)]
+
+
+class Csr(C.Structure):
+    _fields_ = [("nrows", i64), ("ncols", i64), ("nnz", i64),
+                ("row_offsets", vp), ("column_indices", vp), ("values", vp)]
+
+
+class Dia(C.Structure):
+    _fields_ = [("nrows", i64), ("ncols", i64), ("nnz", i64), ("ndiags", i64), ("pitch", i64),
+                ("diagonal_offsets", vp), ("values", vp)]
+
+
+class Ell(C.Structure):
+    _fields_ = [("nrows", i64), ("ncols", i64), ("nnz", i64), ("entries_per_row", i64),
+                ("width", i64), ("pitch", i64), ("column_indices", vp), ("values", vp)]
+
+
+class Hyb(C.Structure):
+    _fields_ = [("ell", Ell), ("coo", Coo)]
+
+
+class Hdc(C.Structure):
+    _fields_ = [("dia", Dia), ("csr", Csr)]
+
+
+# name -> (restype, argtypes)
+_SIGS: dict[str, tuple] = {
+    "mgb_status_string": (C.c_char_p, [C.c_int]),
+    "mgb_version": (C.c_int, []),
+    "mgb_last_cuda_error_string": (C.c_char_p, []),
+}
+for _fmt, _st in (("csr", Csr), ("coo", Coo), ("dia", Dia), ("ell", Ell), ("hyb", Hyb), ("hdc", Hdc)):
+    for _dt in ("f64", "f32"):
+        _SIGS[f"mgb_spmv_{_fmt}_{_dt}"] = (C.c_int, [C.POINTER(_st), vp, vp, C.c_int, vp])
+for _dt, _ct in (("f64", C.c_double), ("f32", C.c_float)):
+    _SIGS[f"mgb_dot_{_dt}"] = (C.c_int, [i64, vp, vp, C.POINTER(_ct), vp])
+    _SIGS[f"mgb_dot_{_dt}_async"] = (C.c_int, [i64, vp, vp, vp, vp])
+    _SIGS[f"mgb_reduce_{_dt}"] = (C.c_int, [vp, i64, C.POINTER(_ct), vp])
+    _SIGS[f"mgb_reduce_{_dt}_async"] = (C.c_int, [vp, i64, vp, vp])
+    _SIGS[f"mgb_waxpby_{_dt}"] = (C.c_int, [i64, _ct, vp, _ct, vp, vp, vp])
+
+
+def load(path: str | None = None):
+    """Load (once) and return the CDLL with prototypes attached."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        p = path or LIB_PATH
+        if not os.path.exists(p):
+            raise ImportError(
+                f"{p} is missing: build it with `python -m morpheus_gb300.build` "
+                "(there is no CPU fallback)")
+        lib = C.CDLL(p)
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+        return lib
+
+
+def call(name: str, *args) -> None:
+    """Call an mgb_* entry point and raise the mapped exception on failure."""
+    lib = load()
+    st = getattr(lib, name)(*args)
+    if st != 0:
+        raise_for_status(st, name, lib.mgb_last_cuda_error_string().decode())
+
+
+def declared_symbols() -> list[str]:
+    return sorted(_SIGS)

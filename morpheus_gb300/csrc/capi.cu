@@ -1,0 +1,56 @@
+// capi.cu -- library-level entry points: status names, version, CUDA error
+// bookkeeping and the cached device query.
+#include <cstdio>
+#include <cstring>
+
+#include "mgb_internal.cuh"
+
+namespace mgb {
+
+static thread_local char g_last_cuda_error[256] = "no error";
+
+int record_cuda_error(cudaError_t e) {
+  std::snprintf(g_last_cuda_error, sizeof(g_last_cuda_error), "%s: %s",
+                cudaGetErrorName(e), cudaGetErrorString(e));
+  return e == cudaErrorMemoryAllocation ? MGB_ERR_ALLOC : MGB_ERR_CUDA;
+}
+
+int num_sms() {
+  static int cache[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 152;
+  if (dev < 0 || dev >= 64) dev = 0;
+  if (cache[dev] == 0) {
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+      n = 152;
+    cache[dev] = n;
+  }
+  return cache[dev];
+}
+
+}  // namespace mgb
+
+extern "C" {
+
+const char* mgb_status_string(int status) {
+  switch (status) {
+    case MGB_SUCCESS: return "MGB_SUCCESS";
+    case MGB_ERR_NOT_IMPLEMENTED: return "MGB_ERR_NOT_IMPLEMENTED (NotImplementedException)";
+    case MGB_ERR_FORMAT_CONVERSION: return "MGB_ERR_FORMAT_CONVERSION (FormatConversionException)";
+    case MGB_ERR_INVALID_INPUT: return "MGB_ERR_INVALID_INPUT (InvalidInputException)";
+    case MGB_ERR_RUNTIME: return "MGB_ERR_RUNTIME (RuntimeException)";
+    case MGB_ERR_IO: return "MGB_ERR_IO (IOException)";
+    case MGB_ERR_CUDA: return "MGB_ERR_CUDA";
+    case MGB_ERR_TIMEOUT: return "MGB_ERR_TIMEOUT";
+    case MGB_ERR_BAD_ARGUMENT: return "MGB_ERR_BAD_ARGUMENT";
+    case MGB_ERR_ALLOC: return "MGB_ERR_ALLOC";
+    default: return "MGB_ERR_UNKNOWN";
+  }
+}
+
+int mgb_version(void) { return 100; /* 0.1.0 */ }
+
+const char* mgb_last_cuda_error_string(void) { return mgb::g_last_cuda_error; }
+
+}  // extern "C"

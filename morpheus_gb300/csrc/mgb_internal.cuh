@@ -1,0 +1,65 @@
+// mgb_internal.cuh -- shared helpers of the morpheus-gb300 CUDA library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/mgb.h"
+
+namespace mgb {
+
+// Records the CUDA error text for mgb_last_cuda_error_string() and returns
+// MGB_ERR_CUDA (or MGB_ERR_ALLOC for an out-of-memory error).
+int record_cuda_error(cudaError_t e);
+
+// Number of SMs of the current device (queried once per device and cached,
+// unlike the reference which queries device properties on every launch,
+// impl/Morpheus_CudaUtils.hpp:77-90).
+int num_sms();
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+}  // namespace mgb
+
+#define MGB_CUDA_CHECK(call)                                  \
+  do {                                                        \
+    cudaError_t mgb_e_ = (call);                              \
+    if (mgb_e_ != cudaSuccess) return ::mgb::record_cuda_error(mgb_e_); \
+  } while (0)
+
+#define MGB_LAUNCH_CHECK() MGB_CUDA_CHECK(cudaGetLastError())
+
+#define MGB_REQUIRE(cond, status) \
+  do {                            \
+    if (!(cond)) return (status); \
+  } while (0)
+
+namespace mgb {
+
+constexpr int WARP = 32;
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// fused multiply-add in the value type (one DFMA / FFMA per nonzero)
+__device__ __forceinline__ double fmadd(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float fmadd(float a, float b, float c) { return fmaf(a, b, c); }
+
+// Read-only, no-L1-allocate streaming loads for matrix data that is used once.
+template <typename T>
+__device__ __forceinline__ T ldg_stream(const T* p) { return __ldcs(p); }
+
+// Launchers shared between translation units (HYB = ELL + COO).
+template <typename T>
+int launch_ell(const mgb_ell* A, const T* x, T* y, int init, cudaStream_t s);
+template <typename T>
+int launch_coo(const mgb_coo* A, const T* x, T* y, int init, cudaStream_t s);
+
+// Validation helpers for descriptors.
+inline bool bad_sizes(int64_t a, int64_t b, int64_t c) { return a < 0 || b < 0 || c < 0; }
+
+}  // namespace mgb

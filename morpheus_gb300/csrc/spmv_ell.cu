@@ -1,0 +1,152 @@
+// spmv_ell.cu -- ELL and HYB SpMV for sm_103a.
+//
+// ELL replaces impl/Ell/Cuda/Morpheus_Multiply_Impl.hpp:41-80 (kernel
+// impl/Ell/Kernels/Morpheus_Multiply_Impl.hpp:37-65).  Semantics are the
+// Serial multiply (impl/Ell/Serial/Morpheus_Multiply_Impl.hpp:38-67): y = 0 if
+// init, then for each row and each of the `width` padded slots whose column
+// is not the invalid index (-1), y[i] += values(i, n) * x[col].
+//
+// HYB replaces impl/Hyb/Cuda/Morpheus_Multiply_Impl.hpp:42-53: the ELL part
+// with init, then the COO part accumulating into y.
+//
+// Layout: slot (i, n) at [i + pitch * n], pitch = nrows (column-major, the
+// reference's CUDA LayoutLeft).  A thread owns RPT consecutive rows and reads
+// each slot column with one 16-byte vector load of column indices and, only
+// where a slot holds an entry, the values (padding values are never read:
+// a warp whose 32*RPT rows are all padding at slot n skips the value sector).
+#include "mgb_internal.cuh"
+
+namespace mgb {
+namespace {
+
+constexpr int ELL_THREADS = 256;
+
+template <typename T, int RPT> struct EllVec;
+template <> struct EllVec<double, 2> {
+  static __device__ __forceinline__ void load(const double* p, double* o) {
+    const double2 v = __ldcs(reinterpret_cast<const double2*>(p)); o[0] = v.x; o[1] = v.y;
+  }
+};
+template <> struct EllVec<float, 2> {
+  static __device__ __forceinline__ void load(const float* p, float* o) {
+    const float2 v = __ldcs(reinterpret_cast<const float2*>(p)); o[0] = v.x; o[1] = v.y;
+  }
+};
+template <typename T> struct EllVec<T, 1> {
+  static __device__ __forceinline__ void load(const T* p, T* o) { o[0] = __ldcs(p); }
+};
+
+template <int RPT> struct IdxVec;
+template <> struct IdxVec<2> {
+  static __device__ __forceinline__ void load(const int32_t* p, int32_t* o) {
+    const int2 v = __ldcs(reinterpret_cast<const int2*>(p)); o[0] = v.x; o[1] = v.y;
+  }
+};
+template <> struct IdxVec<1> {
+  static __device__ __forceinline__ void load(const int32_t* p, int32_t* o) { o[0] = __ldcs(p); }
+};
+
+template <typename T, int RPT>
+__global__ void __launch_bounds__(ELL_THREADS)
+spmv_ell_rows(int64_t nrows, int64_t ncols, int64_t width, int64_t pitch,
+              const int32_t* __restrict__ ci, const T* __restrict__ va,
+              const T* __restrict__ x, T* __restrict__ y, int init) {
+  const int64_t ngroups = (nrows + RPT - 1) / RPT;
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < ngroups;
+       g += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t row0 = g * RPT;
+    const bool full = row0 + RPT <= nrows;
+    T acc[RPT];
+#pragma unroll
+    for (int i = 0; i < RPT; i++) acc[i] = (row0 + i < nrows && !init) ? y[row0 + i] : T(0);
+    for (int64_t n = 0; n < width; n++) {
+      const int64_t base = row0 + pitch * n;
+      int32_t c[RPT];
+      if (full) {
+        IdxVec<RPT>::load(ci + base, c);
+      } else {
+#pragma unroll
+        for (int i = 0; i < RPT; i++) c[i] = (row0 + i < nrows) ? __ldcs(ci + base + i) : -1;
+      }
+      bool any = false;
+#pragma unroll
+      for (int i = 0; i < RPT; i++) any |= ((uint64_t)(int64_t)c[i] < (uint64_t)ncols);
+      if (any) {
+        T v[RPT];
+        if (full) {
+          EllVec<T, RPT>::load(va + base, v);
+        } else {
+#pragma unroll
+          for (int i = 0; i < RPT; i++) v[i] = (row0 + i < nrows) ? __ldcs(va + base + i) : T(0);
+        }
+#pragma unroll
+        for (int i = 0; i < RPT; i++)
+          if ((uint64_t)(int64_t)c[i] < (uint64_t)ncols) acc[i] = fmadd(v[i], __ldg(x + c[i]), acc[i]);
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < RPT; i++)
+      if (row0 + i < nrows) y[row0 + i] = acc[i];
+  }
+}
+
+}  // namespace
+
+template <typename T>
+int launch_ell(const mgb_ell* A, const T* x, T* y, int init, cudaStream_t s) {
+  MGB_REQUIRE(A != nullptr, MGB_ERR_BAD_ARGUMENT);
+  MGB_REQUIRE(!bad_sizes(A->nrows, A->ncols, A->nnz) && A->width >= 0, MGB_ERR_BAD_ARGUMENT);
+  if (A->nrows == 0) return MGB_SUCCESS;
+  MGB_REQUIRE(y != nullptr, MGB_ERR_BAD_ARGUMENT);
+  MGB_REQUIRE(A->width == 0 || (A->pitch >= A->nrows && A->column_indices && A->values && x),
+              MGB_ERR_BAD_ARGUMENT);
+  const bool vec_ok = (A->pitch % 2 == 0) &&
+                      (reinterpret_cast<uintptr_t>(A->values) % (2 * sizeof(T)) == 0) &&
+                      (reinterpret_cast<uintptr_t>(A->column_indices) % 8 == 0);
+  const int rpt = vec_ok ? 2 : 1;
+  const int64_t groups = (A->nrows + rpt - 1) / rpt;
+  int64_t blocks = (groups + ELL_THREADS - 1) / ELL_THREADS;
+  const int64_t cap = (int64_t)num_sms() * 64;
+  if (blocks > cap) blocks = cap;
+  const T* va = static_cast<const T*>(A->values);
+  if (vec_ok)
+    spmv_ell_rows<T, 2><<<(unsigned)blocks, ELL_THREADS, 0, s>>>(
+        A->nrows, A->ncols, A->width, A->pitch, A->column_indices, va, x, y, init);
+  else
+    spmv_ell_rows<T, 1><<<(unsigned)blocks, ELL_THREADS, 0, s>>>(
+        A->nrows, A->ncols, A->width, A->pitch, A->column_indices, va, x, y, init);
+  MGB_LAUNCH_CHECK();
+  return MGB_SUCCESS;
+}
+
+template int launch_ell<double>(const mgb_ell*, const double*, double*, int, cudaStream_t);
+template int launch_ell<float>(const mgb_ell*, const float*, float*, int, cudaStream_t);
+
+template <typename T>
+int launch_hyb(const mgb_hyb* A, const T* x, T* y, int init, cudaStream_t s) {
+  MGB_REQUIRE(A != nullptr, MGB_ERR_BAD_ARGUMENT);
+  MGB_REQUIRE(A->ell.nrows == A->coo.nrows, MGB_ERR_INVALID_INPUT);
+  int st = launch_ell<T>(&A->ell, x, y, init, s);
+  if (st != MGB_SUCCESS) return st;
+  if (A->coo.nnz == 0) return MGB_SUCCESS;
+  return launch_coo<T>(&A->coo, x, y, 0, s);
+}
+
+}  // namespace mgb
+
+extern "C" {
+
+int mgb_spmv_ell_f64(const mgb_ell* A, const double* x, double* y, int init, void* stream) {
+  return mgb::launch_ell<double>(A, x, y, init, mgb::as_stream(stream));
+}
+int mgb_spmv_ell_f32(const mgb_ell* A, const float* x, float* y, int init, void* stream) {
+  return mgb::launch_ell<float>(A, x, y, init, mgb::as_stream(stream));
+}
+int mgb_spmv_hyb_f64(const mgb_hyb* A, const double* x, double* y, int init, void* stream) {
+  return mgb::launch_hyb<double>(A, x, y, init, mgb::as_stream(stream));
+}
+int mgb_spmv_hyb_f32(const mgb_hyb* A, const float* x, float* y, int init, void* stream) {
+  return mgb::launch_hyb<float>(A, x, y, init, mgb::as_stream(stream));
+}
+
+}  // extern "C"

@@ -1,0 +1,216 @@
+// vector_ops.cu -- dot / reduce / waxpby for sm_103a.
+//
+// dot replaces impl/DenseVector/Cuda/Morpheus_Dot_Impl.hpp:59-144 (cuBLAS
+// cublasDdot when enabled -- with the float overload wrongly calling Ddot --
+// else two kernels plus a synchronous copy).  Semantics: Serial dot
+// (impl/DenseVector/Serial/Morpheus_Dot_Impl.hpp:38-59), sum of x[i]*y[i].
+// reduce replaces impl/DenseVector/Cuda/Morpheus_Reduction_Impl.hpp:175-234
+// (multi-pass kernels and a host Kahan finish).  Semantics: the Serial Kahan
+// sum of in[0..size) (impl/DenseVector/Serial/Morpheus_Reduction_Impl.hpp:40-61);
+// here a fixed-shape pairwise tree, deterministic for a given size and GPU.
+// waxpby replaces impl/DenseVector/Cuda/Morpheus_WAXPBY_Impl.hpp:40-70:
+// w = alpha*x + beta*y with the alpha == 1 / beta == 1 special cases of
+// impl/DenseVector/Serial/Morpheus_WAXPBY_Impl.hpp:59-65.
+//
+// Reductions: a grid of at most 4 CTAs per SM accumulates with one FMA (dot)
+// or add (reduce) per element and 16-byte loads, reduces in-CTA with
+// shuffles, and a one-CTA kernel sums the per-CTA partials.  The partials live
+// in stream-ordered scratch (cudaMallocAsync), so no global state is shared
+// between calls or streams.
+#include "mgb_internal.cuh"
+
+namespace mgb {
+namespace {
+
+constexpr int RED_THREADS = 256;
+
+template <typename T>
+__device__ __forceinline__ T block_sum(T v) {
+  __shared__ T s_part[32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  v = warp_sum(v);
+  if (lane == 0) s_part[w] = v;
+  __syncthreads();
+  const int nw = blockDim.x >> 5;
+  v = (threadIdx.x < nw) ? s_part[threadIdx.x] : T(0);
+  if (w == 0) v = warp_sum(v);
+  return v;  // valid in thread 0
+}
+
+// MODE 0: dot(x, y); MODE 1: dot(x, x); MODE 2: sum(x)
+template <typename T, int MODE>
+__global__ void __launch_bounds__(RED_THREADS)
+reduce_partial(int64_t n, const T* __restrict__ x, const T* __restrict__ y,
+               T* __restrict__ partial) {
+  T acc0 = T(0), acc1 = T(0);
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+  // 16-byte vector body when both pointers are 16-byte aligned
+  constexpr int V = 16 / sizeof(T);
+  const bool vec = (reinterpret_cast<uintptr_t>(x) % 16 == 0) &&
+                   (MODE != 0 || reinterpret_cast<uintptr_t>(y) % 16 == 0);
+  int64_t done = 0;
+  if (vec) {
+    const int64_t nv = n / V;
+    for (int64_t i = tid; i < nv; i += nth) {
+      T a[V], b[V];
+      if constexpr (sizeof(T) == 8) {
+        const double2 va = __ldcs(reinterpret_cast<const double2*>(x) + i);
+        a[0] = va.x; a[1] = va.y;
+        if constexpr (MODE == 0) {
+          const double2 vb = __ldcs(reinterpret_cast<const double2*>(y) + i);
+          b[0] = vb.x; b[1] = vb.y;
+        }
+      } else {
+        const float4 va = __ldcs(reinterpret_cast<const float4*>(x) + i);
+        a[0] = va.x; a[1] = va.y; a[2] = va.z; a[3] = va.w;
+        if constexpr (MODE == 0) {
+          const float4 vb = __ldcs(reinterpret_cast<const float4*>(y) + i);
+          b[0] = vb.x; b[1] = vb.y; b[2] = vb.z; b[3] = vb.w;
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < V; k++) {
+        T& acc = (k & 1) ? acc1 : acc0;
+        if (MODE == 0) acc = fmadd(a[k], b[k], acc);
+        else if (MODE == 1) acc = fmadd(a[k], a[k], acc);
+        else acc += a[k];
+      }
+    }
+    done = nv * V;
+  }
+  for (int64_t i = done + tid; i < n; i += nth) {
+    const T a = __ldcs(x + i);
+    if (MODE == 0) acc0 = fmadd(a, __ldcs(y + i), acc0);
+    else if (MODE == 1) acc0 = fmadd(a, a, acc0);
+    else acc0 += a;
+  }
+  const T s = block_sum(acc0 + acc1);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(1024) sum_partials(int n, const T* __restrict__ p, T* __restrict__ out) {
+  T acc = T(0);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) acc += p[i];
+  const T s = block_sum(acc);
+  if (threadIdx.x == 0) *out = s;
+}
+
+template <typename T, int MODE>
+int launch_reduce(int64_t n, const T* x, const T* y, T* d_result, cudaStream_t s) {
+  MGB_REQUIRE(n >= 0 && d_result != nullptr, MGB_ERR_BAD_ARGUMENT);
+  if (n == 0) {
+    MGB_CUDA_CHECK(cudaMemsetAsync(d_result, 0, sizeof(T), s));
+    return MGB_SUCCESS;
+  }
+  MGB_REQUIRE(x != nullptr && (MODE != 0 || y != nullptr), MGB_ERR_BAD_ARGUMENT);
+  int64_t blocks = (n + RED_THREADS * 8 - 1) / (RED_THREADS * 8);
+  const int64_t cap = (int64_t)num_sms() * 4;
+  if (blocks > cap) blocks = cap;
+  T* partial = nullptr;
+  MGB_CUDA_CHECK(cudaMallocAsync((void**)&partial, sizeof(T) * blocks, s));
+  reduce_partial<T, MODE><<<(unsigned)blocks, RED_THREADS, 0, s>>>(n, x, y, partial);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) {
+    sum_partials<T><<<1, 1024, 0, s>>>((int)blocks, partial, d_result);
+    e = cudaGetLastError();
+  }
+  cudaError_t ef = cudaFreeAsync(partial, s);
+  if (e != cudaSuccess) return record_cuda_error(e);
+  if (ef != cudaSuccess) return record_cuda_error(ef);
+  return MGB_SUCCESS;
+}
+
+template <typename T, int MODE>
+int reduce_to_host(int64_t n, const T* x, const T* y, T* result, cudaStream_t s) {
+  MGB_REQUIRE(result != nullptr, MGB_ERR_BAD_ARGUMENT);
+  T* d = nullptr;
+  MGB_CUDA_CHECK(cudaMallocAsync((void**)&d, sizeof(T), s));
+  int st = launch_reduce<T, MODE>(n, x, y, d, s);
+  if (st == MGB_SUCCESS) {
+    cudaError_t e = cudaMemcpyAsync(result, d, sizeof(T), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) st = record_cuda_error(e);
+  }
+  cudaError_t ef = cudaFreeAsync(d, s);
+  if (st == MGB_SUCCESS && ef != cudaSuccess) st = record_cuda_error(ef);
+  return st;
+}
+
+template <typename T>
+int dot_any(int64_t n, const T* x, const T* y, T* out, cudaStream_t s, bool host) {
+  if (x == y) return host ? reduce_to_host<T, 1>(n, x, x, out, s) : launch_reduce<T, 1>(n, x, x, out, s);
+  return host ? reduce_to_host<T, 0>(n, x, y, out, s) : launch_reduce<T, 0>(n, x, y, out, s);
+}
+
+// MODE 0: alpha*x + beta*y, 1: x + beta*y, 2: alpha*x + y
+template <typename T, int MODE>
+__global__ void waxpby_kernel(int64_t n, T alpha, const T* __restrict__ x, T beta,
+                              const T* __restrict__ y, T* __restrict__ w) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const T a = __ldcs(x + i), b = __ldcs(y + i);
+    T r;
+    if (MODE == 1) r = fmadd(beta, b, a);
+    else if (MODE == 2) r = fmadd(alpha, a, b);
+    else r = fmadd(alpha, a, beta * b);
+    __stcs(w + i, r);
+  }
+}
+
+template <typename T>
+int launch_waxpby(int64_t n, T alpha, const T* x, T beta, const T* y, T* w, cudaStream_t s) {
+  MGB_REQUIRE(n >= 0, MGB_ERR_BAD_ARGUMENT);
+  if (n == 0) return MGB_SUCCESS;
+  MGB_REQUIRE(x && y && w, MGB_ERR_BAD_ARGUMENT);
+  int64_t blocks = (n + 255) / 256;
+  const int64_t cap = (int64_t)num_sms() * 16;
+  if (blocks > cap) blocks = cap;
+  if (alpha == T(1))
+    waxpby_kernel<T, 1><<<(unsigned)blocks, 256, 0, s>>>(n, alpha, x, beta, y, w);
+  else if (beta == T(1))
+    waxpby_kernel<T, 2><<<(unsigned)blocks, 256, 0, s>>>(n, alpha, x, beta, y, w);
+  else
+    waxpby_kernel<T, 0><<<(unsigned)blocks, 256, 0, s>>>(n, alpha, x, beta, y, w);
+  MGB_LAUNCH_CHECK();
+  return MGB_SUCCESS;
+}
+
+}  // namespace
+}  // namespace mgb
+
+extern "C" {
+
+int mgb_dot_f64(int64_t n, const double* x, const double* y, double* result, void* stream) {
+  return mgb::dot_any<double>(n, x, y, result, mgb::as_stream(stream), true);
+}
+int mgb_dot_f32(int64_t n, const float* x, const float* y, float* result, void* stream) {
+  return mgb::dot_any<float>(n, x, y, result, mgb::as_stream(stream), true);
+}
+int mgb_dot_f64_async(int64_t n, const double* x, const double* y, double* d_result, void* stream) {
+  return mgb::dot_any<double>(n, x, y, d_result, mgb::as_stream(stream), false);
+}
+int mgb_dot_f32_async(int64_t n, const float* x, const float* y, float* d_result, void* stream) {
+  return mgb::dot_any<float>(n, x, y, d_result, mgb::as_stream(stream), false);
+}
+int mgb_reduce_f64(const double* in, int64_t size, double* result, void* stream) {
+  return mgb::reduce_to_host<double, 2>(size, in, nullptr, result, mgb::as_stream(stream));
+}
+int mgb_reduce_f32(const float* in, int64_t size, float* result, void* stream) {
+  return mgb::reduce_to_host<float, 2>(size, in, nullptr, result, mgb::as_stream(stream));
+}
+int mgb_reduce_f64_async(const double* in, int64_t size, double* d_result, void* stream) {
+  return mgb::launch_reduce<double, 2>(size, in, nullptr, d_result, mgb::as_stream(stream));
+}
+int mgb_reduce_f32_async(const float* in, int64_t size, float* d_result, void* stream) {
+  return mgb::launch_reduce<float, 2>(size, in, nullptr, d_result, mgb::as_stream(stream));
+}
+int mgb_waxpby_f64(int64_t n, double alpha, const double* x, double beta, const double* y, double* w, void* stream) {
+  return mgb::launch_waxpby<double>(n, alpha, x, beta, y, w, mgb::as_stream(stream));
+}
+int mgb_waxpby_f32(int64_t n, float alpha, const float* x, float beta, const float* y, float* w, void* stream) {
+  return mgb::launch_waxpby<float>(n, alpha, x, beta, y, w, mgb::as_stream(stream));
+}
+
+}  // extern "C"

@@ -1,0 +1,1188 @@
+// oracle.cpp -- TEST INFRASTRUCTURE ONLY.
+//
+// A CPU restatement of the Morpheus v0.3.1 Serial (and OpenMP) algorithms on
+// the SpMV hot path.  It is the checker for the CUDA library in
+// morpheus_gb300/: only tests/, __graft_entry__.smoke() and bench.py's CPU
+// baseline leg load it.  Nothing in the product links, imports or calls it.
+//
+// The reference itself cannot be compiled here: every container wraps a
+// Kokkos::View and Kokkos is not installed, so this file restates the
+// algorithms in plain C++17 and is pinned instead against the reference's own
+// golden fixtures (the 10x10 matrix of core/tests/utils/Macros_*.hpp in all six
+// formats, the banded multiply fixtures of core/tests/Test_Multiply.hpp and the
+// dot/reduce known answers of core/tests/Test_{Dot,Reduce}.hpp).
+//
+// Each function names the reference file:line it follows (paths relative to
+// the reference project root).  Loop order, init semantics, padding values,
+// tie-breaks and the exceptions raised are kept, because they define what
+// "the same result" means for the GPU path.  Build flags keep a*b+c as a
+// separately rounded multiply and add (-ffp-contract=off), like the
+// reference's x86 build, so results do not change between x86 and Arm hosts.
+
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <set>
+#include <stdexcept>
+#include <string>
+#include <type_traits>
+#include <variant>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace orc {
+
+// ---------------------------------------------------------------------------
+// Status codes: one per reference exception class
+// (core/src/Morpheus_Exceptions.hpp:32-73).
+// ---------------------------------------------------------------------------
+enum Status {
+  OK                     = 0,
+  NOT_IMPLEMENTED        = 1,
+  FORMAT_CONVERSION      = 2,
+  INVALID_INPUT          = 3,
+  RUNTIME                = 4,
+  BAD_ARGUMENT           = 8,
+};
+
+struct FormatConversionError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+struct InvalidInputError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+struct RuntimeError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+
+enum Format { COO = 0, CSR, DIA, ELL, HYB, HDC, NFORMATS };
+
+using idx_t = int32_t;
+using sz_t  = std::size_t;
+
+// core/src/impl/Dia/Morpheus_Utils_Impl.hpp:33-36
+inline sz_t get_pad_size(sz_t len, sz_t alignment) {
+  return alignment * ((len + alignment - 1) / alignment);
+}
+
+// core/src/impl/Morpheus_Utils.hpp:91-105 -- the fill test is evaluated in
+// single precision, exactly as the reference does.
+inline bool exceeds_tolerance(sz_t num_rows, sz_t num_entries,
+                              sz_t num_columns) {
+  const float max_fill   = 10.0f;
+  const float threshold  = 100e6f;
+  const float size       = float(num_columns) * float(num_rows);
+  const float fill_ratio = size / std::max(1.0f, float(num_entries));
+  return (fill_ratio > max_fill && size > threshold);
+}
+
+// ---------------------------------------------------------------------------
+// Containers.  Dense 2-D slabs are stored column-major with an explicit pitch
+// (the layout the reference uses on CUDA, LayoutLeft); element (i, j) lives at
+// [i + pitch * j].  Layout is not semantics: comparisons are by (i, j).
+// ---------------------------------------------------------------------------
+template <class T>
+struct Coo {  // core/src/Morpheus_CooMatrix.hpp
+  sz_t nrows = 0, ncols = 0, nnz = 0;
+  std::vector<idx_t> row_indices, column_indices;
+  std::vector<T> values;
+  void resize(sz_t r, sz_t c, sz_t n) {
+    nrows = r; ncols = c; nnz = n;
+    row_indices.assign(n, 0); column_indices.assign(n, 0); values.assign(n, T(0));
+  }
+};
+
+template <class T>
+struct Csr {  // core/src/Morpheus_CsrMatrix.hpp:533-537
+  sz_t nrows = 0, ncols = 0, nnz = 0;
+  std::vector<idx_t> row_offsets, column_indices;
+  std::vector<T> values;
+  void resize(sz_t r, sz_t c, sz_t n) {
+    nrows = r; ncols = c; nnz = n;
+    row_offsets.assign(r + 1, 0); column_indices.assign(n, 0); values.assign(n, T(0));
+  }
+};
+
+template <class T>
+struct Dia {  // core/src/Morpheus_DiaMatrix.hpp:192-201, 388-403
+  sz_t nrows = 0, ncols = 0, nnz = 0, ndiags = 0, alignment = 32, pitch = 0;
+  std::vector<idx_t> diagonal_offsets;
+  std::vector<T> values;  // pitch x ndiags, pitch = pad(nrows, alignment)
+  void resize(sz_t r, sz_t c, sz_t n, sz_t nd, sz_t align = 32) {
+    nrows = r; ncols = c; nnz = n; ndiags = nd; alignment = align;
+    if (exceeds_tolerance(r, n, nd))
+      throw FormatConversionError("DiaMatrix fill-in would exceed maximum tolerance");
+    pitch = get_pad_size(r, align);
+    diagonal_offsets.assign(nd, 0);
+    values.assign(pitch * nd, T(0));
+  }
+  T& v(sz_t i, sz_t j) { return values[i + pitch * j]; }
+  const T& v(sz_t i, sz_t j) const { return values[i + pitch * j]; }
+};
+
+template <class T>
+struct Ell {  // core/src/Morpheus_EllMatrix.hpp:189-202, 372-385, 563
+  static constexpr idx_t invalid_index = -1;
+  sz_t nrows = 0, ncols = 0, nnz = 0, entries_per_row = 0, alignment = 32;
+  sz_t width = 0;   // padded slots per row = pad(entries_per_row, alignment)
+  sz_t pitch = 0;   // = nrows (column-major, LayoutLeft)
+  std::vector<idx_t> column_indices;
+  std::vector<T> values;
+  void resize(sz_t r, sz_t c, sz_t n, sz_t epr, sz_t align = 32) {
+    nrows = r; ncols = c; nnz = n; entries_per_row = epr; alignment = align;
+    width = get_pad_size(epr, align);
+    pitch = r;
+    column_indices.assign(pitch * width, 0);
+    values.assign(pitch * width, T(0));
+  }
+  idx_t& ci(sz_t i, sz_t j) { return column_indices[i + pitch * j]; }
+  idx_t ci(sz_t i, sz_t j) const { return column_indices[i + pitch * j]; }
+  T& v(sz_t i, sz_t j) { return values[i + pitch * j]; }
+  const T& v(sz_t i, sz_t j) const { return values[i + pitch * j]; }
+};
+
+template <class T>
+struct Hyb {  // core/src/Morpheus_HybMatrix.hpp:359-376, 473-476
+  sz_t nrows = 0, ncols = 0, nnz = 0, alignment = 32;
+  Ell<T> ell;
+  Coo<T> coo;
+  void resize(sz_t r, sz_t c, sz_t ell_nnz, sz_t coo_nnz, sz_t epr = 0,
+              sz_t align = 32) {
+    nrows = r; ncols = c; nnz = ell_nnz + coo_nnz;
+    sz_t avg = epr;
+    if (epr == 0) avg = (ell_nnz + coo_nnz) / r;
+    ell.resize(r, c, ell_nnz, avg, align);
+    coo.resize(r, c, coo_nnz);
+    alignment = align;
+  }
+};
+
+template <class T>
+struct Hdc {  // core/src/Morpheus_HdcMatrix.hpp:148, 356-367, 464-467
+  static constexpr double true_diagonal_ratio = 0.2;
+  sz_t nrows = 0, ncols = 0, nnz = 0, alignment = 32;
+  Dia<T> dia;
+  Csr<T> csr;
+  void resize(sz_t r, sz_t c, sz_t dia_nnz, sz_t csr_nnz, sz_t nd,
+              sz_t align = 32) {
+    nrows = r; ncols = c; nnz = dia_nnz + csr_nnz;
+    dia.resize(r, c, dia_nnz, nd, align);
+    csr.resize(r, c, csr_nnz);
+    alignment = align;
+  }
+};
+
+template <class T>
+using Dyn = std::variant<Coo<T>, Csr<T>, Dia<T>, Ell<T>, Hyb<T>, Hdc<T>>;
+
+// ---------------------------------------------------------------------------
+// Sort (core/src/impl/Coo/Serial/Morpheus_Sort_Impl.hpp)
+// ---------------------------------------------------------------------------
+
+// :44-60  (starts from numeric_limits<T>::min(), as the reference does)
+inline idx_t find_max_element(const std::vector<idx_t>& v) {
+  idx_t mx = std::numeric_limits<idx_t>::min();
+  for (sz_t i = 0; i < v.size(); i++)
+    if (v[i] > mx) mx = v[i];
+  return mx;
+}
+
+// :62-107  stable counting sort of keys carrying vals
+inline void counting_sort_by_key(std::vector<idx_t>& keys,
+                                 std::vector<idx_t>& vals, idx_t min,
+                                 idx_t max) {
+  if (min < 0)
+    throw InvalidInputError("counting_sort_by_key min element less than 0");
+  if (max < min)
+    throw InvalidInputError("counting_sort_by_key min element less than max element");
+  if (keys.size() < vals.size())
+    throw InvalidInputError("counting_sort_by_key keys.size() less than vals.size()");
+  if (min > 0) min = 0;
+  sz_t size = (sz_t)(max - min);
+  std::vector<idx_t> counts(size + 2, 0);
+  std::vector<idx_t> temp_keys(keys), temp_vals(vals);
+  for (sz_t i = 0; i < keys.size(); i++) counts[keys[i] + 1]++;
+  for (sz_t i = 0; i < size; i++) counts[i + 1] += counts[i];
+  for (sz_t i = 0; i < keys.size(); i++) {
+    keys[counts[temp_keys[i]]]   = temp_keys[i];
+    vals[counts[temp_keys[i]]++] = temp_vals[i];
+  }
+}
+
+// :109-164  two stable passes (by column, then by row) through a permutation
+template <class T>
+void sort_by_row_and_column(Coo<T>& mat) {
+  sz_t N = mat.row_indices.size();
+  std::vector<idx_t> permutation(N);
+  for (sz_t i = 0; i < N; i++) permutation[i] = (idx_t)i;
+  idx_t minr = 0, minc = 0;
+  idx_t maxr = find_max_element(mat.row_indices);
+  idx_t maxc = find_max_element(mat.column_indices);
+  {
+    std::vector<idx_t> temp(mat.column_indices);
+    counting_sort_by_key(temp, permutation, minc, maxc);
+    temp = mat.row_indices;
+    for (sz_t i = 0; i < N; i++) mat.row_indices[i] = temp[permutation[i]];
+    counting_sort_by_key(mat.row_indices, permutation, minr, maxr);
+    temp = mat.column_indices;
+    for (sz_t i = 0; i < N; i++) mat.column_indices[i] = temp[permutation[i]];
+  }
+  {
+    std::vector<T> temp(mat.values);
+    for (sz_t i = 0; i < N; i++) mat.values[i] = temp[permutation[i]];
+  }
+}
+
+// :166-186  (callers never reach it with nnz == 0)
+template <class T>
+bool is_sorted(const Coo<T>& mat) {
+  if (mat.row_indices.size() != mat.column_indices.size())
+    throw RuntimeError("Sizes of row and column indeces do not match.");
+  if (mat.nnz == 0) return true;
+  for (sz_t i = 0; i < mat.nnz - 1; i++) {
+    if ((mat.row_indices[i] > mat.row_indices[i + 1]) ||
+        (mat.row_indices[i] == mat.row_indices[i + 1] &&
+         mat.column_indices[i] > mat.column_indices[i + 1]))
+      return false;
+  }
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// Analytics
+// ---------------------------------------------------------------------------
+
+// core/src/impl/Coo/Kokkos/Morpheus_NonZeros_Per_Diagonal_Impl.hpp:38-78
+template <class T>
+void count_nnz_per_diagonal(const Coo<T>& A, std::vector<idx_t>& out,
+                            bool init) {
+  if (init) std::fill(out.begin(), out.end(), 0);
+  for (sz_t i = 0; i < A.nnz; i++) {
+    sz_t idx = (sz_t)((int64_t)A.column_indices[i] - A.row_indices[i] +
+                      (int64_t)A.nrows - 1);
+    out[idx]++;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Conversions (Serial).  Every pair goes through COO like the reference's
+// generic hub core/src/impl/Morpheus_Convert_Impl.hpp:82-104.
+// ---------------------------------------------------------------------------
+
+// core/src/impl/Csr/Serial/Morpheus_Convert_Impl.hpp:70-97  CSR -> COO
+template <class T>
+void convert(const Csr<T>& src, Coo<T>& dst) {
+  dst.resize(src.nrows, src.ncols, src.nnz);
+  for (sz_t i = 0; i < src.nrows; i++)
+    for (idx_t jj = src.row_offsets[i]; jj < src.row_offsets[i + 1]; jj++)
+      dst.row_indices[jj] = (idx_t)i;
+  for (sz_t n = 0; n < src.nnz; n++) dst.column_indices[n] = src.column_indices[n];
+  for (sz_t n = 0; n < src.nnz; n++) dst.values[n] = src.values[n];
+}
+
+// core/src/impl/Csr/Serial/Morpheus_Convert_Impl.hpp:99-151  COO -> CSR
+// (counting scatter: stable within a row, keeps COO order)
+template <class T>
+void convert(const Coo<T>& src, Csr<T>& dst) {
+  dst.resize(src.nrows, src.ncols, src.nnz);
+  std::fill(dst.row_offsets.begin(), dst.row_offsets.end(), 0);
+  for (sz_t n = 0; n < src.nnz; n++) dst.row_offsets[src.row_indices[n]]++;
+  idx_t cumsum = 0;
+  for (sz_t i = 0; i < src.nrows; i++) {
+    idx_t temp          = dst.row_offsets[i];
+    dst.row_offsets[i]  = cumsum;
+    cumsum += temp;
+  }
+  dst.row_offsets[src.nrows] = (idx_t)src.nnz;
+  for (sz_t n = 0; n < src.nnz; n++) {
+    sz_t row  = (sz_t)src.row_indices[n];
+    sz_t dest = (sz_t)dst.row_offsets[row];
+    dst.column_indices[dest] = src.column_indices[n];
+    dst.values[dest]         = src.values[n];
+    dst.row_offsets[row]++;
+  }
+  idx_t last = 0;
+  for (sz_t i = 0; i <= src.nrows; i++) {
+    idx_t temp         = dst.row_offsets[i];
+    dst.row_offsets[i] = last;
+    last               = temp;
+  }
+}
+
+// core/src/impl/Dia/Serial/Morpheus_Convert_Impl.hpp:72-118  DIA -> COO
+// Exact zeros stored in the slab are dropped; the COO keeps the DIA's nnz, so
+// any unfilled tail entries stay (0, 0, 0) and the sort moves them first.
+template <class T>
+void convert(const Dia<T>& src, Coo<T>& dst) {
+  dst.resize(src.nrows, src.ncols, src.nnz);
+  if (src.nnz == 0) return;
+  const sz_t ndiag = src.diagonal_offsets.size();
+  for (sz_t i = 0, nnzid = 0; i < ndiag; i++) {
+    const idx_t k       = src.diagonal_offsets[i];
+    const sz_t i_start  = (sz_t)std::max<idx_t>(0, -k);
+    const sz_t j_start  = (sz_t)std::max<idx_t>(0, k);
+    const sz_t N = std::min(src.nrows - i_start, src.ncols - j_start);
+    for (sz_t n = 0; n < N; n++) {
+      const T temp = src.v(i_start + n, i);
+      if (temp != T(0)) {
+        dst.row_indices[nnzid]    = (idx_t)(i_start + n);
+        dst.column_indices[nnzid] = (idx_t)(j_start + n);
+        dst.values[nnzid]         = temp;
+        nnzid                     = nnzid + 1;
+      }
+    }
+  }
+  if (!is_sorted(dst)) sort_by_row_and_column(dst);
+}
+
+// core/src/impl/Dia/Serial/Morpheus_Convert_Impl.hpp:120-169  COO -> DIA
+template <class T>
+void convert(const Coo<T>& src, Dia<T>& dst) {
+  if (src.nnz == 0) {
+    dst.resize(src.nrows, src.ncols, src.nnz, 0);
+    return;
+  }
+  std::vector<idx_t> diag_map(src.nnz, 0);
+  for (sz_t n = 0; n < src.nnz; n++)
+    diag_map[n] = src.column_indices[n] - src.row_indices[n];
+  std::set<idx_t> diag_set(diag_map.begin(), diag_map.end());
+  sz_t ndiags = diag_set.size();
+  if (exceeds_tolerance(src.nrows, src.nnz, ndiags))
+    throw FormatConversionError("DiaMatrix fill-in would exceed maximum tolerance");
+  dst.resize(src.nrows, src.ncols, src.nnz, ndiags);
+  sz_t i = 0;
+  for (auto it = diag_set.cbegin(); it != diag_set.cend(); ++it, ++i)
+    dst.diagonal_offsets[i] = *it;
+  for (sz_t n = 0; n < src.nnz; n++) {
+    for (sz_t d = 0; d < ndiags; d++) {
+      if (diag_map[n] == dst.diagonal_offsets[d]) {
+        dst.v((sz_t)src.row_indices[n], d) = src.values[n];
+        break;
+      }
+    }
+  }
+}
+
+// core/src/impl/Ell/Serial/Morpheus_Convert_Impl.hpp:68-109  ELL -> COO
+template <class T>
+void convert(const Ell<T>& src, Coo<T>& dst) {
+  dst.resize(src.nrows, src.ncols, src.nnz);
+  if (src.nnz == 0) return;
+  sz_t num_entries = 0;
+  const sz_t num_entries_per_row = src.width;
+  for (sz_t i = 0; i < src.nrows; i++) {
+    for (sz_t n = 0; n < num_entries_per_row; n++) {
+      const idx_t j = src.ci(i, n);
+      const T v     = src.v(i, n);
+      if (j != Ell<T>::invalid_index) {
+        dst.row_indices[num_entries]    = (idx_t)i;
+        dst.column_indices[num_entries] = j;
+        dst.values[num_entries]         = v;
+        num_entries++;
+      }
+    }
+  }
+  if (!is_sorted(dst)) sort_by_row_and_column(dst);
+}
+
+// core/src/impl/Ell/Serial/Morpheus_Convert_Impl.hpp:111-173  COO -> ELL
+// W = the longest row; slots fill in COO order; padding = (-1, 0).
+template <class T>
+void convert(const Coo<T>& src, Ell<T>& dst) {
+  std::vector<idx_t> row_offsets(src.nrows + 1, 0);
+  for (sz_t n = 0; n < src.nnz; n++) row_offsets[src.row_indices[n]]++;
+  idx_t cumsum = 0;
+  for (sz_t i = 0; i < src.nrows; i++) {
+    idx_t temp     = row_offsets[i];
+    row_offsets[i] = cumsum;
+    cumsum += temp;
+  }
+  row_offsets[src.nrows] = (idx_t)src.nnz;
+  sz_t num_entries_per_row = 0;
+  for (sz_t i = 0; i < src.nrows; i++) {
+    sz_t e = (sz_t)(row_offsets[i + 1] - row_offsets[i]);
+    num_entries_per_row = e > num_entries_per_row ? e : num_entries_per_row;
+  }
+  if (exceeds_tolerance(src.nrows, src.nnz, num_entries_per_row))
+    throw FormatConversionError("EllMatrix fill-in would exceed maximum tolerance");
+  dst.resize(src.nrows, src.ncols, src.nnz, num_entries_per_row);
+  std::fill(dst.column_indices.begin(), dst.column_indices.end(), Ell<T>::invalid_index);
+  std::fill(dst.values.begin(), dst.values.end(), T(0));
+  idx_t row_id = 0;
+  for (sz_t i = 0, n = 0; i < src.nnz; i++) {
+    idx_t row = src.row_indices[i];
+    if (row_id != src.row_indices[i]) {
+      n      = 0;
+      row_id = src.row_indices[i];
+    }
+    dst.ci((sz_t)row, n) = src.column_indices[i];
+    dst.v((sz_t)row, n)  = src.values[i];
+    n++;
+  }
+}
+
+// core/src/impl/Hyb/Serial/Morpheus_Convert_Impl.hpp:62-108  HYB -> COO
+template <class T>
+void convert(const Hyb<T>& src, Coo<T>& dst) {
+  dst.resize(src.nrows, src.ncols, src.nnz);
+  if (src.nnz == 0) return;
+  const sz_t num_entries_per_row = src.ell.width;
+  sz_t num_entries = 0, coo_progress = 0;
+  for (sz_t i = 0; i < src.nrows; i++) {
+    for (sz_t n = 0; n < num_entries_per_row; n++) {
+      if (src.ell.ci(i, n) != Ell<T>::invalid_index) {
+        dst.row_indices[num_entries]    = (idx_t)i;
+        dst.column_indices[num_entries] = src.ell.ci(i, n);
+        dst.values[num_entries]         = src.ell.v(i, n);
+        num_entries++;
+      }
+    }
+    while ((coo_progress < src.coo.nnz) &&
+           ((sz_t)src.coo.row_indices[coo_progress] == i)) {
+      dst.row_indices[num_entries]    = (idx_t)i;
+      dst.column_indices[num_entries] = src.coo.column_indices[coo_progress];
+      dst.values[num_entries]         = src.coo.values[coo_progress];
+      num_entries++;
+      coo_progress++;
+    }
+  }
+  if (!is_sorted(dst)) sort_by_row_and_column(dst);
+}
+
+// core/src/impl/Hyb/Serial/Morpheus_Convert_Impl.hpp:110-196  COO -> HYB
+// ELL width = max(1, nnz / nrows) (integer mean); the first W entries of each
+// row go to ELL, the rest to COO, both in COO order.
+template <class T>
+void convert(const Coo<T>& src, Hyb<T>& dst, sz_t forced_width = 0) {
+  const sz_t alignment = 32;
+  sz_t num_entries_per_row =
+      std::max<sz_t>(1, src.nrows ? src.nnz / src.nrows : 0);
+  if (forced_width) num_entries_per_row = forced_width;
+  std::vector<idx_t> row_offsets(src.nrows + 1, 0);
+  for (sz_t n = 0; n < src.nnz; n++) row_offsets[src.row_indices[n]]++;
+  idx_t cumsum = 0;
+  for (sz_t i = 0; i < src.nrows; i++) {
+    idx_t temp     = row_offsets[i];
+    row_offsets[i] = cumsum;
+    cumsum += temp;
+  }
+  row_offsets[src.nrows] = (idx_t)src.nnz;
+  sz_t num_ell_entries = 0;
+  for (sz_t i = 0; i < src.nrows; i++) {
+    sz_t e = (sz_t)(row_offsets[i + 1] - row_offsets[i]);
+    num_ell_entries += e > num_entries_per_row ? num_entries_per_row : e;
+  }
+  if (exceeds_tolerance(src.nrows, num_ell_entries, num_entries_per_row))
+    throw FormatConversionError("EllMatrix fill-in would exceed maximum tolerance");
+  sz_t num_coo_entries = src.nnz - num_ell_entries;
+  dst.resize(src.nrows, src.ncols, num_ell_entries, num_coo_entries,
+             num_entries_per_row, alignment);
+  std::fill(dst.ell.column_indices.begin(), dst.ell.column_indices.end(),
+            Ell<T>::invalid_index);
+  std::fill(dst.ell.values.begin(), dst.ell.values.end(), T(0));
+  idx_t row_id = 0;
+  sz_t coo_nnz = 0;
+  for (sz_t i = 0, n = 0; i < src.nnz; i++) {
+    idx_t row = src.row_indices[i];
+    if (row_id != src.row_indices[i]) {
+      n      = 0;
+      row_id = src.row_indices[i];
+    }
+    if ((n < num_entries_per_row) && (row_id == src.row_indices[i])) {
+      dst.ell.ci((sz_t)row, n) = src.column_indices[i];
+      dst.ell.v((sz_t)row, n)  = src.values[i];
+      n++;
+    } else if (row_id == src.row_indices[i]) {
+      dst.coo.row_indices[coo_nnz]    = src.row_indices[i];
+      dst.coo.column_indices[coo_nnz] = src.column_indices[i];
+      dst.coo.values[coo_nnz]         = src.values[i];
+      coo_nnz++;
+    }
+  }
+}
+
+// core/src/impl/Hdc/Serial/Morpheus_Convert_Impl.hpp:64-130  HDC -> COO
+template <class T>
+void convert(const Hdc<T>& src, Coo<T>& dst) {
+  dst.resize(src.nrows, src.ncols, src.nnz);
+  if (src.nnz == 0) return;
+  const sz_t ndiag = src.dia.ndiags;
+  sz_t nnzid = 0;
+  for (sz_t i = 0; i < ndiag; i++) {
+    const idx_t k      = src.dia.diagonal_offsets[i];
+    const sz_t i_start = (sz_t)std::max<idx_t>(0, -k);
+    const sz_t j_start = (sz_t)std::max<idx_t>(0, k);
+    const sz_t N = std::min(src.nrows - i_start, src.ncols - j_start);
+    for (sz_t n = 0; n < N; n++) {
+      const T temp = src.dia.v(i_start + n, i);
+      if (temp != T(0)) {
+        dst.row_indices[nnzid]    = (idx_t)(i_start + n);
+        dst.column_indices[nnzid] = (idx_t)(j_start + n);
+        dst.values[nnzid]         = temp;
+        nnzid++;
+      }
+    }
+  }
+  for (sz_t i = 0; i < src.csr.nrows; i++)
+    for (idx_t jj = src.csr.row_offsets[i]; jj < src.csr.row_offsets[i + 1]; jj++)
+      dst.row_indices[jj + nnzid] = (idx_t)i;
+  for (sz_t n = 0; n < src.csr.nnz; n++)
+    dst.column_indices[n + nnzid] = src.csr.column_indices[n];
+  for (sz_t n = 0; n < src.csr.nnz; n++) dst.values[n + nnzid] = src.csr.values[n];
+  if (!is_sorted(dst)) sort_by_row_and_column(dst);
+}
+
+// core/src/impl/Hdc/Serial/Morpheus_Convert_Impl.hpp:132-226  COO -> HDC
+// Diagonals holding >= floor(0.2 * nrows) entries go to DIA (offsets sorted),
+// the rest to CSR in COO order.  The midpoint bin is recorded as offset 0,
+// which is the true diagonal only for square matrices (kept as written).
+template <class T>
+void convert(const Coo<T>& src, Hdc<T>& dst) {
+  const double true_diag_ratio = Hdc<T>::true_diagonal_ratio;
+  idx_t min_diag_elem = (idx_t)(src.nrows * true_diag_ratio);
+  std::vector<idx_t> nnz_per_diag(src.nrows + src.ncols - 1, 0);
+  std::vector<idx_t> bit_map(nnz_per_diag.size(), 0);
+  count_nnz_per_diagonal(src, nnz_per_diag, false);
+  sz_t ndiags = 0, dia_nnz = 0, csr_nnz = 0;
+  for (sz_t i = 0; i < nnz_per_diag.size(); i++) {
+    if (nnz_per_diag[i] >= min_diag_elem) {
+      ndiags++;
+      dia_nnz += nnz_per_diag[i];
+      bit_map[i] = 1;
+    } else if ((nnz_per_diag[i] < min_diag_elem) && (nnz_per_diag[i] != 0)) {
+      csr_nnz += nnz_per_diag[i];
+    }
+  }
+  if (exceeds_tolerance(src.nrows, dia_nnz, ndiags))
+    throw FormatConversionError("DiaMatrix fill-in would exceed maximum tolerance");
+  const sz_t alignment = 32;
+  dst.resize(src.nrows, src.ncols, dia_nnz, csr_nnz, ndiags, alignment);
+  std::fill(dst.csr.row_offsets.begin(), dst.csr.row_offsets.end(), 0);
+  int nnz_mid_point = (int)nnz_per_diag.size() / 2;
+  int dia_ctr = 0;
+  for (int i = nnz_mid_point - 1; i >= 0; i--)
+    if (bit_map[i]) dst.dia.diagonal_offsets[dia_ctr++] = i - (int)src.nrows + 1;
+  if (bit_map[nnz_mid_point]) dst.dia.diagonal_offsets[dia_ctr++] = 0;
+  for (int i = nnz_mid_point + 1; i < (int)nnz_per_diag.size(); i++)
+    if (bit_map[i]) dst.dia.diagonal_offsets[dia_ctr++] = i - (int)src.nrows + 1;
+  std::sort(dst.dia.diagonal_offsets.begin(), dst.dia.diagonal_offsets.end());
+  sz_t csr_entries = 0;
+  for (sz_t n = 0; n < src.nnz; n++) {
+    bool dia_entry = false;
+    for (sz_t i = 0; i < ndiags; i++) {
+      if (src.column_indices[n] - src.row_indices[n] ==
+          dst.dia.diagonal_offsets[i]) {
+        dst.dia.v((sz_t)src.row_indices[n], i) = src.values[n];
+        dia_entry = true;
+        break;
+      }
+    }
+    if (!dia_entry) {
+      // The reference writes past the CSR part here when a non-square
+      // matrix has a true diagonal in the midpoint bin (undefined behaviour);
+      // the oracle reports it instead.
+      if (csr_entries >= csr_nnz)
+        throw RuntimeError("HDC CSR part overflow (non-square midpoint diagonal)");
+      dst.csr.row_offsets[src.row_indices[n]]++;
+      dst.csr.column_indices[csr_entries] = src.column_indices[n];
+      dst.csr.values[csr_entries]         = src.values[n];
+      csr_entries++;
+    }
+  }
+  idx_t cumsum = 0;
+  for (sz_t i = 0; i < src.nrows; i++) {
+    idx_t temp              = dst.csr.row_offsets[i];
+    dst.csr.row_offsets[i]  = cumsum;
+    cumsum += temp;
+  }
+  dst.csr.row_offsets[src.nrows] = (idx_t)csr_nnz;
+}
+
+// Same-format copies (core/src/impl/<Fmt>/Serial/Morpheus_Convert_Impl.hpp,
+// first overload in each file): element-wise copy.
+template <class M>
+void copy_same(const M& src, M& dst) { dst = src; }
+
+template <class T> void to_coo(const Coo<T>& s, Coo<T>& d) { copy_same(s, d); }
+template <class T> void to_coo(const Csr<T>& s, Coo<T>& d) { convert(s, d); }
+template <class T> void to_coo(const Dia<T>& s, Coo<T>& d) { convert(s, d); }
+template <class T> void to_coo(const Ell<T>& s, Coo<T>& d) { convert(s, d); }
+template <class T> void to_coo(const Hyb<T>& s, Coo<T>& d) { convert(s, d); }
+template <class T> void to_coo(const Hdc<T>& s, Coo<T>& d) { convert(s, d); }
+
+template <class T> void from_coo(const Coo<T>& s, Coo<T>& d) { copy_same(s, d); }
+template <class T> void from_coo(const Coo<T>& s, Csr<T>& d) { convert(s, d); }
+template <class T> void from_coo(const Coo<T>& s, Dia<T>& d) { convert(s, d); }
+template <class T> void from_coo(const Coo<T>& s, Ell<T>& d) { convert(s, d); }
+template <class T> void from_coo(const Coo<T>& s, Hyb<T>& d) { convert(s, d); }
+template <class T> void from_coo(const Coo<T>& s, Hdc<T>& d) { convert(s, d); }
+
+// core/src/impl/Morpheus_Convert_Impl.hpp:82-104 (X -> COO -> Y) and the
+// Dynamic visits of core/src/impl/Dynamic/Morpheus_Convert_Impl.hpp:46-84.
+template <class T>
+void convert_any(const Dyn<T>& src, Dyn<T>& dst) {
+  if (src.index() == dst.index()) {
+    dst = src;
+    return;
+  }
+  Coo<T> tmp;
+  std::visit([&](const auto& s) { to_coo(s, tmp); }, src);
+  std::visit([&](auto& d) { from_coo(tmp, d); }, dst);
+}
+
+template <class T>
+Dyn<T> make_empty(int fmt) {
+  switch (fmt) {
+    case COO: return Coo<T>();
+    case CSR: return Csr<T>();
+    case DIA: return Dia<T>();
+    case ELL: return Ell<T>();
+    case HYB: return Hyb<T>();
+    default: return Hdc<T>();
+  }
+}
+
+// core/src/Morpheus_Convert.hpp:88-124  in-place convert of a DynamicMatrix
+// returns conversion_error_e {DYNAMIC_TO_PROXY=0, PROXY_TO_DYNAMIC, CONV_SUCCESS}
+template <class T>
+int convert_inplace(Dyn<T>& src, int index) {
+  if ((int)src.index() == index) return 2;
+  Coo<T> temp;
+  if (src.index() != COO) {
+    try {
+      std::visit([&](const auto& s) { to_coo(s, temp); }, src);
+    } catch (...) {
+      return 0;
+    }
+  } else {
+    temp = std::get<Coo<T>>(src);
+  }
+  Dyn<T> dynamic_temp = make_empty<T>(index);
+  try {
+    std::visit([&](auto& d) { from_coo(temp, d); }, dynamic_temp);
+  } catch (...) {
+    return 1;
+  }
+  src = dynamic_temp;
+  return 2;
+}
+
+// ---------------------------------------------------------------------------
+// Multiply (Serial restatements; product = separately rounded mult and add)
+// ---------------------------------------------------------------------------
+
+// core/src/impl/Csr/Serial/Morpheus_Multiply_Impl.hpp:38-58
+template <class T>
+void multiply(const Csr<T>& A, const T* x, T* y, bool init) {
+  for (sz_t i = 0; i < A.nrows; i++) {
+    T sum = init ? T(0) : y[i];
+    for (idx_t jj = A.row_offsets[i]; jj < A.row_offsets[i + 1]; jj++)
+      sum += A.values[jj] * x[A.column_indices[jj]];
+    y[i] = sum;
+  }
+}
+
+// core/src/impl/Coo/Serial/Morpheus_Multiply_Impl.hpp:38-59
+template <class T>
+void multiply(const Coo<T>& A, const T* x, T* y, bool init) {
+  if (init)
+    for (sz_t n = 0; n < A.nrows; n++) y[n] = T(0);
+  for (sz_t n = 0; n < A.nnz; n++)
+    y[A.row_indices[n]] += A.values[n] * x[A.column_indices[n]];
+}
+
+// core/src/impl/Dia/Serial/Morpheus_Multiply_Impl.hpp:38-64
+template <class T>
+void multiply(const Dia<T>& A, const T* x, T* y, bool init) {
+  const sz_t ndiag = A.ndiags;
+  for (sz_t row = 0; row < A.nrows; row++) {
+    T sum = init ? T(0) : y[row];
+    for (sz_t n = 0; n < ndiag; n++) {
+      const int64_t col = (int64_t)row + A.diagonal_offsets[n];
+      if (col >= 0 && col < (int64_t)A.ncols) sum += A.v(row, n) * x[col];
+    }
+    y[row] = sum;
+  }
+}
+
+// core/src/impl/Ell/Serial/Morpheus_Multiply_Impl.hpp:38-67
+template <class T>
+void multiply(const Ell<T>& A, const T* x, T* y, bool init) {
+  const sz_t num_entries_per_row = A.width;
+  if (init)
+    for (sz_t n = 0; n < A.nrows; n++) y[n] = T(0);
+  for (sz_t i = 0; i < A.nrows; i++)
+    for (sz_t n = 0; n < num_entries_per_row; n++)
+      if (A.ci(i, n) != Ell<T>::invalid_index)
+        y[i] += A.v(i, n) * x[A.ci(i, n)];
+}
+
+// core/src/impl/Hyb/Serial/Morpheus_Multiply_Impl.hpp:41-52  (ELL init, COO accumulate)
+template <class T>
+void multiply(const Hyb<T>& A, const T* x, T* y, bool init) {
+  multiply(A.ell, x, y, init);
+  multiply(A.coo, x, y, false);
+}
+
+// core/src/impl/Hdc/Serial/Morpheus_Multiply_Impl.hpp:41-52  (DIA init, CSR accumulate)
+template <class T>
+void multiply(const Hdc<T>& A, const T* x, T* y, bool init) {
+  multiply(A.dia, x, y, init);
+  multiply(A.csr, x, y, false);
+}
+
+// ---------------------------------------------------------------------------
+// Multiply (OpenMP restatements; the timed CPU baseline)
+// ---------------------------------------------------------------------------
+
+// core/src/impl/Csr/OpenMP/Morpheus_Multiply_Impl.hpp:37-58
+template <class T>
+void multiply_omp(const Csr<T>& A, const T* x, T* y, bool init) {
+  const int64_t nrows = (int64_t)A.nrows;
+#pragma omp parallel for
+  for (int64_t i = 0; i < nrows; i++) {
+    T sum = init ? T(0) : y[i];
+    for (idx_t jj = A.row_offsets[i]; jj < A.row_offsets[i + 1]; jj++)
+      sum += A.values[jj] * x[A.column_indices[jj]];
+    y[i] = sum;
+  }
+}
+
+// core/src/impl/Coo/OpenMP/Morpheus_Multiply_Impl.hpp:42-107
+// equal nnz split per thread; rows shared with a neighbour go through an
+// atomic add of the partial sum.
+template <class T>
+void multiply_omp(const Coo<T>& A, const T* x, T* y, bool init) {
+  const int64_t nrows = (int64_t)A.nrows;
+  if (init) {
+#pragma omp parallel for
+    for (int64_t n = 0; n < nrows; n++) y[n] = T(0);
+  }
+  const sz_t nnnz = A.nnz;
+  const idx_t sentinel_row = (idx_t)(A.nrows + 1);
+  const idx_t* rind = A.row_indices.data();
+  const idx_t* cind = A.column_indices.data();
+  const T* Aval = A.values.data();
+#pragma omp parallel
+  {
+#ifdef _OPENMP
+    const sz_t num_threads = (sz_t)omp_get_num_threads();
+    const sz_t thread_id   = (sz_t)omp_get_thread_num();
+#else
+    const sz_t num_threads = 1, thread_id = 0;
+#endif
+    const sz_t work_per_thread = (nnnz + num_threads - 1) / num_threads;
+    const sz_t begin = work_per_thread * thread_id;
+    const sz_t end   = std::min(begin + work_per_thread, nnnz);
+    sz_t n = begin;
+    if (begin < end) {
+      const idx_t first = begin > 0 ? rind[begin - 1] : sentinel_row;
+      const idx_t last  = end < nnnz ? rind[end] : sentinel_row;
+      if (first != sentinel_row) {
+        T partial = T(0);
+        for (; n < end && rind[n] == first; n++) partial += Aval[n] * x[cind[n]];
+#pragma omp atomic
+        y[first] += partial;
+      }
+      for (; n < end && rind[n] != last; n++) y[rind[n]] += Aval[n] * x[cind[n]];
+      if (last != sentinel_row) {
+        T partial = T(0);
+        for (; n < end; n++) partial += Aval[n] * x[cind[n]];
+#pragma omp atomic
+        y[last] += partial;
+      }
+    }
+  }
+}
+
+// core/src/impl/Dia/OpenMP/Morpheus_Multiply_Impl.hpp:40-66
+template <class T>
+void multiply_omp(const Dia<T>& A, const T* x, T* y, bool init) {
+  const int64_t nrows = (int64_t)A.nrows;
+  const sz_t ndiag = A.ndiags;
+#pragma omp parallel for
+  for (int64_t row = 0; row < nrows; row++) {
+    T sum = init ? T(0) : y[row];
+    for (sz_t n = 0; n < ndiag; n++) {
+      const int64_t col = row + A.diagonal_offsets[n];
+      if (col >= 0 && col < (int64_t)A.ncols) sum += A.v((sz_t)row, n) * x[col];
+    }
+    y[row] = sum;
+  }
+}
+
+// core/src/impl/Ell/OpenMP/Morpheus_Multiply_Impl.hpp:40-71
+template <class T>
+void multiply_omp(const Ell<T>& A, const T* x, T* y, bool init) {
+  const int64_t nrows = (int64_t)A.nrows;
+  const sz_t W = A.width;
+  if (init) {
+#pragma omp parallel for
+    for (int64_t n = 0; n < nrows; n++) y[n] = T(0);
+  }
+#pragma omp parallel for
+  for (int64_t i = 0; i < nrows; i++)
+    for (sz_t n = 0; n < W; n++)
+      if (A.ci((sz_t)i, n) != Ell<T>::invalid_index)
+        y[i] += A.v((sz_t)i, n) * x[A.ci((sz_t)i, n)];
+}
+
+// core/src/impl/Hyb/OpenMP/Morpheus_Multiply_Impl.hpp (ELL then COO)
+template <class T>
+void multiply_omp(const Hyb<T>& A, const T* x, T* y, bool init) {
+  multiply_omp(A.ell, x, y, init);
+  multiply_omp(A.coo, x, y, false);
+}
+
+// core/src/impl/Hdc/OpenMP/Morpheus_Multiply_Impl.hpp (DIA then CSR)
+template <class T>
+void multiply_omp(const Hdc<T>& A, const T* x, T* y, bool init) {
+  multiply_omp(A.dia, x, y, init);
+  multiply_omp(A.csr, x, y, false);
+}
+
+// ---------------------------------------------------------------------------
+// Dense vector ops (Serial)
+// ---------------------------------------------------------------------------
+
+// core/src/impl/DenseVector/Serial/Morpheus_Dot_Impl.hpp:38-59
+template <class T>
+T dot(sz_t n, const T* x, const T* y) {
+  T result = T(0);
+  if (y == x) {
+    for (sz_t i = 0; i < n; i++) result += x[i] * x[i];
+  } else {
+    for (sz_t i = 0; i < n; i++) result += x[i] * y[i];
+  }
+  return result;
+}
+
+// core/src/impl/DenseVector/Serial/Morpheus_Reduction_Impl.hpp:40-61 (Kahan)
+template <class T>
+T reduce(const T* in, sz_t size) {
+  T sum = in[0];
+  T c   = T(0);
+  for (sz_t i = 1; i < size; i++) {
+    T y = in[i] - c;
+    T t = sum + y;
+    c   = (t - sum) - y;
+    sum = t;
+  }
+  return sum;
+}
+
+// core/src/impl/DenseVector/Serial/Morpheus_WAXPBY_Impl.hpp:39-67
+template <class T>
+void waxpby(sz_t n, T alpha, const T* x, T beta, const T* y, T* w) {
+  if (alpha == T(1.0)) {
+    for (sz_t i = 0; i < n; i++) w[i] = x[i] + beta * y[i];
+  } else if (beta == T(1.0)) {
+    for (sz_t i = 0; i < n; i++) w[i] = alpha * x[i] + y[i];
+  } else {
+    for (sz_t i = 0; i < n; i++) w[i] = alpha * x[i] + beta * y[i];
+  }
+}
+
+}  // namespace orc
+
+// ===========================================================================
+// C interface (loaded with ctypes by oracle/oracle.py)
+// ===========================================================================
+using namespace orc;
+
+struct Handle {
+  int dtype;  // 0 = double, 1 = float
+  Dyn<double> d;
+  Dyn<float> f;
+};
+
+template <class F>
+static int guarded(F&& fn) {
+  try {
+    fn();
+    return OK;
+  } catch (const FormatConversionError&) {
+    return FORMAT_CONVERSION;
+  } catch (const InvalidInputError&) {
+    return INVALID_INPUT;
+  } catch (const RuntimeError&) {
+    return RUNTIME;
+  } catch (const std::bad_variant_access&) {
+    return BAD_ARGUMENT;
+  } catch (...) {
+    return RUNTIME;
+  }
+}
+
+template <class Fn>
+static auto with_dyn(Handle* h, Fn&& fn) {
+  if (h->dtype == 0) return fn(h->d);
+  return fn(h->f);
+}
+
+// Named-array access.  A name selects one array of the active container:
+// COO: row_indices column_indices values; CSR: row_offsets column_indices
+// values; DIA: diagonal_offsets values; ELL: column_indices values;
+// HYB: ell.column_indices ell.values coo.row_indices coo.column_indices
+// coo.values; HDC: dia.diagonal_offsets dia.values csr.row_offsets
+// csr.column_indices csr.values.
+template <class T>
+static std::vector<idx_t>* idx_array(Dyn<T>& d, const std::string& name) {
+  switch (d.index()) {
+    case COO: {
+      auto& m = std::get<Coo<T>>(d);
+      if (name == "row_indices") return &m.row_indices;
+      if (name == "column_indices") return &m.column_indices;
+      break;
+    }
+    case CSR: {
+      auto& m = std::get<Csr<T>>(d);
+      if (name == "row_offsets") return &m.row_offsets;
+      if (name == "column_indices") return &m.column_indices;
+      break;
+    }
+    case DIA: {
+      auto& m = std::get<Dia<T>>(d);
+      if (name == "diagonal_offsets") return &m.diagonal_offsets;
+      break;
+    }
+    case ELL: {
+      auto& m = std::get<Ell<T>>(d);
+      if (name == "column_indices") return &m.column_indices;
+      break;
+    }
+    case HYB: {
+      auto& m = std::get<Hyb<T>>(d);
+      if (name == "ell.column_indices") return &m.ell.column_indices;
+      if (name == "coo.row_indices") return &m.coo.row_indices;
+      if (name == "coo.column_indices") return &m.coo.column_indices;
+      break;
+    }
+    case HDC: {
+      auto& m = std::get<Hdc<T>>(d);
+      if (name == "dia.diagonal_offsets") return &m.dia.diagonal_offsets;
+      if (name == "csr.row_offsets") return &m.csr.row_offsets;
+      if (name == "csr.column_indices") return &m.csr.column_indices;
+      break;
+    }
+  }
+  return nullptr;
+}
+
+template <class T>
+static std::vector<T>* val_array(Dyn<T>& d, const std::string& name) {
+  switch (d.index()) {
+    case COO: if (name == "values") return &std::get<Coo<T>>(d).values; break;
+    case CSR: if (name == "values") return &std::get<Csr<T>>(d).values; break;
+    case DIA: if (name == "values") return &std::get<Dia<T>>(d).values; break;
+    case ELL: if (name == "values") return &std::get<Ell<T>>(d).values; break;
+    case HYB:
+      if (name == "ell.values") return &std::get<Hyb<T>>(d).ell.values;
+      if (name == "coo.values") return &std::get<Hyb<T>>(d).coo.values;
+      break;
+    case HDC:
+      if (name == "dia.values") return &std::get<Hdc<T>>(d).dia.values;
+      if (name == "csr.values") return &std::get<Hdc<T>>(d).csr.values;
+      break;
+  }
+  return nullptr;
+}
+
+// shape vector: [fmt, nrows, ncols, nnz, a, b, c, d, e, f]
+//   DIA: a=ndiags b=pitch c=alignment
+//   ELL: a=entries_per_row b=width c=pitch d=alignment
+//   HYB: a=ell.entries_per_row b=ell.width c=ell.pitch d=ell.nnz e=coo.nnz f=alignment
+//   HDC: a=dia.ndiags b=dia.pitch c=dia.nnz d=csr.nnz e=alignment
+template <class T>
+static void get_shape(const Dyn<T>& d, int64_t* s) {
+  for (int i = 0; i < 10; i++) s[i] = 0;
+  s[0] = (int64_t)d.index();
+  std::visit([&](const auto& m) { s[1] = m.nrows; s[2] = m.ncols; s[3] = m.nnz; }, d);
+  switch (d.index()) {
+    case DIA: { auto& m = std::get<Dia<T>>(d); s[4] = m.ndiags; s[5] = m.pitch; s[6] = m.alignment; break; }
+    case ELL: { auto& m = std::get<Ell<T>>(d); s[4] = m.entries_per_row; s[5] = m.width; s[6] = m.pitch; s[7] = m.alignment; break; }
+    case HYB: { auto& m = std::get<Hyb<T>>(d); s[4] = m.ell.entries_per_row; s[5] = m.ell.width; s[6] = m.ell.pitch; s[7] = m.ell.nnz; s[8] = m.coo.nnz; s[9] = m.alignment; break; }
+    case HDC: { auto& m = std::get<Hdc<T>>(d); s[4] = m.dia.ndiags; s[5] = m.dia.pitch; s[6] = m.dia.nnz; s[7] = m.csr.nnz; s[8] = m.alignment; break; }
+  }
+}
+
+// resize the active container (the reference resize() of each format)
+template <class T>
+static void do_resize(Dyn<T>& d, const int64_t* s) {
+  sz_t r = (sz_t)s[1], c = (sz_t)s[2], n = (sz_t)s[3];
+  switch (d.index()) {
+    case COO: std::get<Coo<T>>(d).resize(r, c, n); break;
+    case CSR: std::get<Csr<T>>(d).resize(r, c, n); break;
+    case DIA: std::get<Dia<T>>(d).resize(r, c, n, (sz_t)s[4], s[6] ? (sz_t)s[6] : 32); break;
+    case ELL: std::get<Ell<T>>(d).resize(r, c, n, (sz_t)s[4], s[7] ? (sz_t)s[7] : 32); break;
+    case HYB: std::get<Hyb<T>>(d).resize(r, c, (sz_t)s[7], (sz_t)s[8], (sz_t)s[4], s[9] ? (sz_t)s[9] : 32); break;
+    case HDC: std::get<Hdc<T>>(d).resize(r, c, (sz_t)s[6], (sz_t)s[7], (sz_t)s[4], s[8] ? (sz_t)s[8] : 32); break;
+  }
+}
+
+extern "C" {
+
+void* orc_new(int fmt, int dtype) {
+  if (fmt < 0 || fmt >= NFORMATS || dtype < 0 || dtype > 1) return nullptr;
+  Handle* h = new Handle();
+  h->dtype = dtype;
+  h->d = make_empty<double>(fmt);
+  h->f = make_empty<float>(fmt);
+  return h;
+}
+
+void orc_free(void* p) { delete static_cast<Handle*>(p); }
+
+void* orc_clone(void* p) { return new Handle(*static_cast<Handle*>(p)); }
+
+int orc_format(void* p) {
+  Handle* h = static_cast<Handle*>(p);
+  return with_dyn(h, [](auto& d) { return (int)d.index(); });
+}
+
+// DynamicMatrix::activate (core/src/Morpheus_DynamicMatrix.hpp:409-442):
+// resets to an EMPTY container of the new format; an index past the last
+// format is a no-op.
+int orc_activate(void* p, int fmt) {
+  Handle* h = static_cast<Handle*>(p);
+  if (fmt < 0 || fmt >= NFORMATS) return BAD_ARGUMENT;
+  if (h->dtype == 0) h->d = make_empty<double>(fmt);
+  else h->f = make_empty<float>(fmt);
+  return OK;
+}
+
+int orc_shape(void* p, int64_t* s) {
+  Handle* h = static_cast<Handle*>(p);
+  with_dyn(h, [&](auto& d) { get_shape(d, s); return 0; });
+  return OK;
+}
+
+int orc_resize(void* p, const int64_t* s) {
+  Handle* h = static_cast<Handle*>(p);
+  return guarded([&] { with_dyn(h, [&](auto& d) { do_resize(d, s); return 0; }); });
+}
+
+// pointer + length of a named array (length in elements; -1 if unknown name)
+int64_t orc_array(void* p, const char* name, void** out) {
+  Handle* h = static_cast<Handle*>(p);
+  std::string nm(name);
+  return with_dyn(h, [&](auto& d) -> int64_t {
+    if (auto* a = idx_array(d, nm)) { *out = a->data(); return (int64_t)a->size(); }
+    if (auto* a = val_array(d, nm)) { *out = a->data(); return (int64_t)a->size(); }
+    *out = nullptr;
+    return -1;
+  });
+}
+
+// Morpheus::convert<Serial>(src, dst): dst's active format is the target.
+int orc_convert(void* src, void* dst) {
+  Handle* s = static_cast<Handle*>(src);
+  Handle* d = static_cast<Handle*>(dst);
+  if (s->dtype != d->dtype) return BAD_ARGUMENT;
+  return guarded([&] {
+    if (s->dtype == 0) convert_any(s->d, d->d);
+    else convert_any(s->f, d->f);
+  });
+}
+
+// COO -> HYB with an explicit ELL width (a width other than the reference's
+// integer mean; same placement rule).
+int orc_coo_to_hyb_width(void* src, void* dst, int64_t width) {
+  Handle* s = static_cast<Handle*>(src);
+  Handle* d = static_cast<Handle*>(dst);
+  if (s->dtype != d->dtype) return BAD_ARGUMENT;
+  return guarded([&] {
+    if (s->dtype == 0) {
+      Hyb<double> out;
+      convert(std::get<Coo<double>>(s->d), out, (sz_t)width);
+      d->d = out;
+    } else {
+      Hyb<float> out;
+      convert(std::get<Coo<float>>(s->f), out, (sz_t)width);
+      d->f = out;
+    }
+  });
+}
+
+// Morpheus::convert<Serial>(dyn, formats_e) -> conversion_error_e
+int orc_convert_inplace(void* p, int fmt) {
+  Handle* h = static_cast<Handle*>(p);
+  if (h->dtype == 0) return convert_inplace(h->d, fmt);
+  return convert_inplace(h->f, fmt);
+}
+
+int orc_sort_by_row_and_column(void* p) {
+  Handle* h = static_cast<Handle*>(p);
+  return guarded([&] {
+    if (h->dtype == 0) sort_by_row_and_column(std::get<Coo<double>>(h->d));
+    else sort_by_row_and_column(std::get<Coo<float>>(h->f));
+  });
+}
+
+int orc_is_sorted(void* p) {
+  Handle* h = static_cast<Handle*>(p);
+  if (h->dtype == 0) return is_sorted(std::get<Coo<double>>(h->d)) ? 1 : 0;
+  return is_sorted(std::get<Coo<float>>(h->f)) ? 1 : 0;
+}
+
+int orc_count_nnz_per_diagonal(void* p, int32_t* out) {
+  Handle* h = static_cast<Handle*>(p);
+  return guarded([&] {
+    with_dyn(h, [&](auto& d) {
+      auto& m = std::get<0>(d);
+      std::vector<idx_t> v(m.nrows + m.ncols - 1, 0);
+      count_nnz_per_diagonal(m, v, true);
+      std::memcpy(out, v.data(), v.size() * sizeof(idx_t));
+      return 0;
+    });
+  });
+}
+
+// multiply: threads == 0 runs the Serial restatement, threads > 0 the OpenMP
+// restatement on that many threads.
+int orc_multiply(void* p, const void* x, void* y, int init, int threads) {
+  Handle* h = static_cast<Handle*>(p);
+  return guarded([&] {
+    auto run = [&](auto& d, auto* xx, auto* yy) {
+      if (threads <= 0) {
+        std::visit([&](const auto& A) { multiply(A, xx, yy, init != 0); }, d);
+      } else {
+#ifdef _OPENMP
+        omp_set_num_threads(threads);
+#endif
+        std::visit([&](const auto& A) { multiply_omp(A, xx, yy, init != 0); }, d);
+      }
+    };
+    if (h->dtype == 0) run(h->d, (const double*)x, (double*)y);
+    else run(h->f, (const float*)x, (float*)y);
+  });
+}
+
+double orc_dot_f64(int64_t n, const double* x, const double* y) { return dot<double>((sz_t)n, x, y); }
+float orc_dot_f32(int64_t n, const float* x, const float* y) { return dot<float>((sz_t)n, x, y); }
+double orc_reduce_f64(const double* x, int64_t n) { return reduce<double>(x, (sz_t)n); }
+float orc_reduce_f32(const float* x, int64_t n) { return reduce<float>(x, (sz_t)n); }
+void orc_waxpby_f64(int64_t n, double a, const double* x, double b, const double* y, double* w) {
+  waxpby<double>((sz_t)n, a, x, b, y, w);
+}
+void orc_waxpby_f32(int64_t n, float a, const float* x, float b, const float* y, float* w) {
+  waxpby<float>((sz_t)n, a, x, b, y, w);
+}
+
+int orc_exceeds_tolerance(int64_t nrows, int64_t nnz, int64_t ncols) {
+  return exceeds_tolerance((sz_t)nrows, (sz_t)nnz, (sz_t)ncols) ? 1 : 0;
+}
+
+int orc_max_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+}  // extern "C"

@@ -1,0 +1,56 @@
+"""CPU: the C-ABI library builds for sm_103a, loads without a GPU, exports every
+symbol include/mgb.h declares, and rejects bad arguments before touching CUDA."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+from morpheus_gb300 import _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_symbols():
+    text = open(os.path.join(ROOT, "include", "mgb.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(mgb_\w+)\s*\(", text, re.M)))
+
+
+def test_library_exports_every_declared_symbol(lib_built):
+    lib = C.CDLL(lib_built)
+    missing = [s for s in header_symbols() if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_bindings_cover_header(lib_built):
+    assert set(_lib.declared_symbols()) == set(header_symbols())
+
+
+def test_status_strings_and_version(lib_built):
+    lib = _lib.load()
+    assert lib.mgb_version() >= 100
+    assert b"FormatConversionException" in lib.mgb_status_string(2)
+    assert lib.mgb_status_string(0) == b"MGB_SUCCESS"
+
+
+@pytest.mark.parametrize("fmt", ["csr", "coo", "dia", "ell", "hyb", "hdc"])
+@pytest.mark.parametrize("dt", ["f64", "f32"])
+def test_null_descriptor_is_rejected(lib_built, fmt, dt):
+    lib = _lib.load()
+    fn = getattr(lib, f"mgb_spmv_{fmt}_{dt}")
+    assert fn(None, None, None, 1, None) == 8  # MGB_ERR_BAD_ARGUMENT
+
+
+def test_negative_sizes_rejected(lib_built):
+    lib = _lib.load()
+    d = _lib.Csr(-1, 4, 0, None, None, None)
+    assert lib.mgb_spmv_csr_f64(C.byref(d), None, None, 1, None) == 8
+    assert lib.mgb_waxpby_f64(-5, 1.0, None, 1.0, None, None, None) == 8
+    out = C.c_double()
+    assert lib.mgb_dot_f64(10, None, None, C.byref(out), None) != 0
+
+
+def test_empty_matrix_is_a_noop_without_gpu(lib_built):
+    lib = _lib.load()
+    d = _lib.Csr(0, 0, 0, None, None, None)
+    assert lib.mgb_spmv_csr_f64(C.byref(d), None, None, 1, None) == 0

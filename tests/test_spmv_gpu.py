@@ -1,0 +1,179 @@
+"""GPU parity: every SpMV kernel, FP64 and FP32, against the oracle's Serial
+multiply on identical inputs, through the C ABI (morpheus_gb300.multiply).
+
+Bar: normwise relative error ||y - y_oracle|| / ||y_oracle|| <= 1e-12 (FP64)
+and <= 1e-5 (FP32, against both the FP32 and the FP64 oracle).  The kernels
+use fused multiply-add and a different summation order for rows split across
+lanes, so y is compared by tolerance, not bitwise.
+"""
+import numpy as np
+import pytest
+import torch
+
+import morpheus_gb300 as mgb
+from helpers import FORMATS, golden, rel_err
+from morpheus_gb300 import generators as gen
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+TOL = {np.float64: 1e-12, np.float32: 1e-5}
+
+
+def gpu_multiply(hm, x, y0, init):
+    A = mgb.matrix_from_host(hm, device="cuda")
+    xt = torch.from_numpy(x).cuda()
+    yt = torch.from_numpy(y0.copy()).cuda()
+    mgb.multiply(A, xt, yt, init=init)
+    torch.cuda.synchronize()
+    return yt.cpu().numpy()
+
+
+def check(hm, dtype, init=True, seed=0):
+    n, m = hm["nrows"], hm["ncols"]
+    x = gen.x_vector(m, seed=seed, dtype=dtype)
+    y0 = gen.x_vector(n, seed=seed + 1, dtype=dtype)
+    om = O.OracleMatrix.from_host(hm)
+    ref = om.multiply(x, y0.copy(), init=init)
+    y = gpu_multiply(hm, x, y0, init)
+    err = rel_err(y, ref)
+    assert err <= TOL[dtype], f"rel err {err:.3e}"
+    if dtype == np.float32:  # also against the FP64 oracle on the same inputs
+        hm64 = _cast(hm, np.float64)
+        ref64 = O.OracleMatrix.from_host(hm64).multiply(x.astype(np.float64), y0.astype(np.float64),
+                                                        init=init)
+        assert rel_err(y, ref64) <= TOL[np.float32]
+    return err
+
+
+def _cast(hm, dtype):
+    out = {}
+    for k, v in hm.items():
+        if isinstance(v, dict):
+            out[k] = _cast(v, dtype)
+        elif isinstance(v, np.ndarray) and v.dtype.kind == "f":
+            out[k] = v.astype(dtype)
+        else:
+            out[k] = v
+    return out
+
+
+def all_formats(csr_hm, hyb_width=None):
+    """The six containers of one matrix, built by the oracle's convert."""
+    om = O.OracleMatrix.from_host(csr_hm)
+    out = {}
+    for f, name in enumerate(FORMATS):
+        try:
+            out[name] = om.convert(f).to_host()
+        except O.OracleError:
+            pass  # fill tolerance exceeded: the reference refuses this format too
+    if hyb_width is not None:
+        out["HYB_W"] = om.convert(O.COO).coo_to_hyb(hyb_width).to_host()
+    return out
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("fmt", FORMATS)
+@pytest.mark.parametrize("init", [True, False])
+def test_golden_small_matrix(cuda, fmt, dtype, init):
+    check(golden(dtype)[fmt], dtype, init)
+
+
+@pytest.mark.parametrize("N", [10, 100, 1000])
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_banded(cuda, N, dtype):
+    for name, hm in all_formats(gen.banded(N, seed=N, dtype=dtype)).items():
+        for init in (True, False):
+            check(hm, dtype, init)
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_power_law_small(cuda, dtype):
+    A = gen.power_law(30000, seed=3, dtype=dtype)
+    p90 = int(np.percentile(np.diff(A["row_offsets"]), 90))
+    for name, hm in all_formats(A, hyb_width=p90).items():
+        for init in (True, False):
+            check(hm, dtype, init)
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_stencil_and_hdc(cuda, dtype):
+    S = gen.stencil_27pt(24, seed=4, dtype=dtype)
+    for name, hm in all_formats(S).items():
+        check(hm, dtype, True)
+    H = gen.add_offband(S, 0.01, seed=5)
+    hdc = O.OracleMatrix.from_host(H).convert(O.HDC).to_host()
+    assert hdc["csr"]["nnz"] > 0 and hdc["dia"]["ndiags"] == 27
+    for init in (True, False):
+        check(hdc, dtype, init)
+
+
+def test_laplacian_all_formats(cuda):
+    for name, hm in all_formats(gen.laplacian_2d(64)).items():
+        check(hm, np.float64, True)
+
+
+@pytest.mark.parametrize("case", ["empty_rows", "leading_trailing_empty", "one_long_row",
+                                  "tiny", "rows_longer_than_chunk", "all_empty", "nonsquare"])
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_edge_cases(cuda, case, dtype):
+    if case == "empty_rows":
+        A = gen.random_csr(5000, 5000, 0.002, seed=7, dtype=dtype, empty_row_frac=0.5)
+    elif case == "leading_trailing_empty":
+        lens = np.zeros(3000, dtype=np.int64)
+        lens[1000:2000] = 5
+        A = gen.random_lengths_csr(3000, 3000, lens, seed=8, dtype=dtype)
+    elif case == "one_long_row":
+        lens = np.ones(2000, dtype=np.int64)
+        lens[777] = 60000
+        A = gen.random_lengths_csr(2000, 100000, lens, seed=9, dtype=dtype)
+    elif case == "tiny":
+        A = gen.random_lengths_csr(3, 3, np.array([1, 0, 2]), seed=10, dtype=dtype)
+    elif case == "rows_longer_than_chunk":
+        A = gen.random_lengths_csr(64, 20000, np.full(64, 5000), seed=11, dtype=dtype)
+    elif case == "all_empty":
+        A = gen.random_lengths_csr(100, 100, np.zeros(100, dtype=np.int64), seed=12, dtype=dtype)
+    else:
+        A = gen.random_csr(700, 2300, 0.01, seed=13, dtype=dtype)
+    for name, hm in all_formats(A).items():
+        for init in (True, False):
+            if hm["nnz"] == 0 and name in ("DIA", "HDC") and hm["nrows"] == 0:
+                continue
+            check(hm, dtype, init)
+
+
+def test_deterministic(cuda):
+    A = gen.power_law(50000, seed=14)
+    x = gen.x_vector(A["ncols"], seed=1)
+    for name, hm in all_formats(A).items():
+        y1 = gpu_multiply(hm, x, np.zeros(A["nrows"]), True)
+        y2 = gpu_multiply(hm, x, np.zeros(A["nrows"]), True)
+        assert np.array_equal(y1, y2), name
+
+
+def test_dynamic_matrix_dispatch(cuda):
+    g = golden()
+    x = gen.x_vector(10, seed=2)
+    ref = O.OracleMatrix.from_host(g["CSR"]).multiply(x)
+    for name in FORMATS:
+        dyn = mgb.DynamicMatrix(mgb.matrix_from_host(g[name]))
+        assert dyn.active_index() == FORMATS.index(name)
+        y = torch.zeros(10, dtype=torch.float64, device="cuda")
+        mgb.multiply(dyn, torch.from_numpy(x).cuda(), y)
+        assert rel_err(y.cpu().numpy(), ref) <= 1e-12
+
+
+def test_host_container_is_rejected(cuda):
+    A = mgb.matrix_from_host(golden()["CSR"], device="cpu")
+    x = torch.zeros(10, dtype=torch.float64, device="cuda")
+    with pytest.raises(mgb.NotImplementedException):
+        mgb.multiply(A, x, x.clone())
+
+
+@pytest.mark.slow
+def test_power_law_full_size(cuda):
+    """Full power-law size (N = 2e6): FP64 CSR against the OpenMP oracle."""
+    A = gen.power_law(2_000_000, seed=0)
+    x = gen.x_vector(A["ncols"], seed=0)
+    ref = O.OracleMatrix.from_host(A).multiply(x, threads=O.max_threads())
+    y = gpu_multiply(A, x, np.zeros(A["nrows"]), True)
+    assert rel_err(y, ref) <= 1e-12
