@@ -1,0 +1,545 @@
+// Morpheus_GB300.hpp -- header-only C++17 front end of morpheus-gb300.
+//
+// Keeps the reference's template API for the SpMV hot path so that code
+// written against Morpheus switches by changing the execution space:
+//
+//   Morpheus::CsrMatrix<double> A(...);                 // device containers
+//   Morpheus::multiply<Morpheus::GB300>(A, x, y);       // core/src/Morpheus_Multiply.hpp:57-78
+//   Morpheus::multiply<Morpheus::GB300>(A, x, y, false);// y += A*x
+//   double d = Morpheus::dot<Morpheus::GB300>(n, x, y); // core/src/Morpheus_Dot.hpp:50-58
+//   double s = Morpheus::reduce<Morpheus::GB300>(x, n); // core/src/Morpheus_Reduction.hpp:46-52
+//   Morpheus::waxpby<Morpheus::GB300>(n, a, x, b, y, w);// core/src/Morpheus_WAXPBY.hpp:52-64
+//   Morpheus::convert<Morpheus::GB300>(src, dst);       // core/src/Morpheus_Convert.hpp:53-57
+//   Morpheus::convert<Morpheus::GB300>(dyn, fmt);       // core/src/Morpheus_Convert.hpp:88-141
+//
+// Containers own device memory (RAII over cudaMalloc) and expose the
+// reference's accessors (nrows(), ncols(), nnnz(), row_offsets(), ...).
+// Every algorithm calls the C ABI of mgb.h; a non-success status is rethrown
+// as the reference's exception class (core/src/Morpheus_Exceptions.hpp:32-73).
+#ifndef MORPHEUS_GB300_HPP
+#define MORPHEUS_GB300_HPP
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <type_traits>
+#include <utility>
+#include <variant>
+#include <vector>
+
+#include "mgb.h"
+
+namespace Morpheus {
+
+// ---------------------------------------------------------------- spaces ---
+// The GB300 execution space: algorithms templated on it run the sm_103a
+// kernels of libmorpheus_gb300.so on the current CUDA device.
+struct GB300 {
+  using execution_space = GB300;
+};
+
+// ----------------------------------------------------------- exceptions ---
+class Exception : public std::exception {
+ public:
+  explicit Exception(std::string m) : message(std::move(m)) {}
+  const char* what() const noexcept override { return message.c_str(); }
+
+ protected:
+  std::string message;
+};
+class NotImplementedException : public Exception {
+ public:
+  explicit NotImplementedException(const std::string& fn)
+      : Exception("NotImplemented: " + fn + " not yet implemented.") {}
+};
+class IOException : public Exception {
+ public:
+  explicit IOException(const std::string& m) : Exception("IO: " + m) {}
+};
+class RuntimeException : public Exception {
+ public:
+  explicit RuntimeException(const std::string& m) : Exception(m) {}
+};
+class InvalidInputException : public Exception {
+ public:
+  explicit InvalidInputException(const std::string& m) : Exception(m) {}
+};
+class FormatConversionException : public Exception {
+ public:
+  explicit FormatConversionException(const std::string& m) : Exception(m) {}
+};
+
+namespace Impl {
+inline void check(int st, const char* where) {
+  if (st == MGB_SUCCESS) return;
+  std::string msg = std::string(where) + ": " + mgb_status_string(st);
+  if (st == MGB_ERR_CUDA || st == MGB_ERR_ALLOC) msg += std::string(" (") + mgb_last_cuda_error_string() + ")";
+  switch (st) {
+    case MGB_ERR_NOT_IMPLEMENTED: throw NotImplementedException(where);
+    case MGB_ERR_FORMAT_CONVERSION: throw FormatConversionException(msg);
+    case MGB_ERR_INVALID_INPUT:
+    case MGB_ERR_BAD_ARGUMENT: throw InvalidInputException(msg);
+    case MGB_ERR_IO: throw IOException(msg);
+    default: throw RuntimeException(msg);
+  }
+}
+inline void cuda_check(cudaError_t e, const char* where) {
+  if (e != cudaSuccess) throw RuntimeException(std::string(where) + ": " + cudaGetErrorString(e));
+}
+inline int64_t get_pad_size(int64_t len, int64_t alignment) {  // impl/Dia/Morpheus_Utils_Impl.hpp:33-36
+  return alignment * ((len + alignment - 1) / alignment);
+}
+}  // namespace Impl
+
+// ------------------------------------------------------------- enums ---
+enum formats_e { COO_FORMAT = 0, CSR_FORMAT, DIA_FORMAT, ELL_FORMAT, HYB_FORMAT, HDC_FORMAT, NFORMATS };
+enum conversion_error_e { DYNAMIC_TO_PROXY = 0, PROXY_TO_DYNAMIC, CONV_SUCCESS };
+
+// ------------------------------------------------------- device buffer ---
+template <class T>
+class DeviceArray {
+ public:
+  DeviceArray() = default;
+  explicit DeviceArray(size_t n, T fill = T(0)) { resize(n, fill); }
+  explicit DeviceArray(const std::vector<T>& host) { assign(host); }
+  DeviceArray(const DeviceArray& o) { *this = o; }
+  DeviceArray(DeviceArray&& o) noexcept : ptr_(o.ptr_), n_(o.n_) { o.ptr_ = nullptr; o.n_ = 0; }
+  DeviceArray& operator=(const DeviceArray& o) {  // deep copy (device to device)
+    if (this != &o) {
+      alloc(o.n_);
+      if (n_) Impl::cuda_check(cudaMemcpy(ptr_, o.ptr_, n_ * sizeof(T), cudaMemcpyDeviceToDevice), "copy");
+    }
+    return *this;
+  }
+  DeviceArray& operator=(DeviceArray&& o) noexcept {
+    std::swap(ptr_, o.ptr_);
+    std::swap(n_, o.n_);
+    return *this;
+  }
+  ~DeviceArray() { release(); }
+
+  void resize(size_t n, T fill = T(0)) {
+    alloc(n);
+    if (n_) assign_fill(fill);
+  }
+  void assign(const std::vector<T>& host) {
+    alloc(host.size());
+    if (n_) Impl::cuda_check(cudaMemcpy(ptr_, host.data(), n_ * sizeof(T), cudaMemcpyHostToDevice), "upload");
+  }
+  std::vector<T> to_host() const {
+    std::vector<T> h(n_);
+    if (n_) Impl::cuda_check(cudaMemcpy(h.data(), ptr_, n_ * sizeof(T), cudaMemcpyDeviceToHost), "download");
+    return h;
+  }
+  T* data() { return ptr_; }
+  const T* data() const { return ptr_; }
+  size_t size() const { return n_; }
+
+ private:
+  void alloc(size_t n) {
+    if (n == n_) return;
+    release();
+    if (n) Impl::cuda_check(cudaMalloc((void**)&ptr_, n * sizeof(T)), "cudaMalloc");
+    n_ = n;
+  }
+  void release() {
+    if (ptr_) cudaFree(ptr_);
+    ptr_ = nullptr;
+    n_ = 0;
+  }
+  void assign_fill(T fill) {
+    if (fill == T(0)) {
+      Impl::cuda_check(cudaMemset(ptr_, 0, n_ * sizeof(T)), "memset");
+    } else {
+      std::vector<T> h(n_, fill);
+      Impl::cuda_check(cudaMemcpy(ptr_, h.data(), n_ * sizeof(T), cudaMemcpyHostToDevice), "fill");
+    }
+  }
+  T* ptr_ = nullptr;
+  size_t n_ = 0;
+};
+
+// ---------------------------------------------------------- DenseVector ---
+// core/src/Morpheus_DenseVector.hpp (device space)
+template <class ValueType>
+class DenseVector {
+ public:
+  using value_type = ValueType;
+  DenseVector() = default;
+  explicit DenseVector(size_t n, ValueType v = ValueType(0)) : a_(n, v) {}
+  explicit DenseVector(const std::vector<ValueType>& h) : a_(h) {}
+  size_t size() const { return a_.size(); }
+  ValueType* data() { return a_.data(); }
+  const ValueType* data() const { return a_.data(); }
+  void assign(size_t n, ValueType v) { a_.resize(n, v); }
+  std::vector<ValueType> to_host() const { return a_.to_host(); }
+
+ private:
+  DeviceArray<ValueType> a_;
+};
+
+// ------------------------------------------------------------ matrices ---
+template <class ValueType>
+class CooMatrix {  // core/src/Morpheus_CooMatrix.hpp
+ public:
+  using value_type = ValueType;
+  static constexpr formats_e format = COO_FORMAT;
+  CooMatrix() = default;
+  CooMatrix(int64_t r, int64_t c, int64_t n) { resize(r, c, n); }
+  CooMatrix(int64_t r, int64_t c, const std::vector<int32_t>& ri, const std::vector<int32_t>& ci,
+            const std::vector<ValueType>& v)
+      : nrows_(r), ncols_(c), nnz_((int64_t)v.size()), ri_(ri), ci_(ci), v_(v) {}
+  void resize(int64_t r, int64_t c, int64_t n) {
+    nrows_ = r; ncols_ = c; nnz_ = n;
+    ri_.resize(n); ci_.resize(n); v_.resize(n);
+  }
+  int64_t nrows() const { return nrows_; }
+  int64_t ncols() const { return ncols_; }
+  int64_t nnnz() const { return nnz_; }
+  formats_e format_enum() const { return format; }
+  int format_index() const { return format; }
+  DeviceArray<int32_t>& row_indices() { return ri_; }
+  DeviceArray<int32_t>& column_indices() { return ci_; }
+  DeviceArray<ValueType>& values() { return v_; }
+  const DeviceArray<int32_t>& crow_indices() const { return ri_; }
+  const DeviceArray<int32_t>& ccolumn_indices() const { return ci_; }
+  const DeviceArray<ValueType>& cvalues() const { return v_; }
+  mgb_coo desc() const {
+    return mgb_coo{nrows_, ncols_, nnz_, const_cast<int32_t*>(ri_.data()), const_cast<int32_t*>(ci_.data()),
+                   const_cast<ValueType*>(v_.data())};
+  }
+
+ private:
+  int64_t nrows_ = 0, ncols_ = 0, nnz_ = 0;
+  DeviceArray<int32_t> ri_, ci_;
+  DeviceArray<ValueType> v_;
+};
+
+template <class ValueType>
+class CsrMatrix {  // core/src/Morpheus_CsrMatrix.hpp:533-537
+ public:
+  using value_type = ValueType;
+  static constexpr formats_e format = CSR_FORMAT;
+  CsrMatrix() = default;
+  CsrMatrix(int64_t r, int64_t c, int64_t n) { resize(r, c, n); }
+  CsrMatrix(int64_t r, int64_t c, const std::vector<int32_t>& ro, const std::vector<int32_t>& ci,
+            const std::vector<ValueType>& v)
+      : nrows_(r), ncols_(c), nnz_((int64_t)v.size()), ro_(ro), ci_(ci), v_(v) {}
+  void resize(int64_t r, int64_t c, int64_t n) {
+    nrows_ = r; ncols_ = c; nnz_ = n;
+    ro_.resize(r + 1); ci_.resize(n); v_.resize(n);
+  }
+  int64_t nrows() const { return nrows_; }
+  int64_t ncols() const { return ncols_; }
+  int64_t nnnz() const { return nnz_; }
+  formats_e format_enum() const { return format; }
+  int format_index() const { return format; }
+  DeviceArray<int32_t>& row_offsets() { return ro_; }
+  DeviceArray<int32_t>& column_indices() { return ci_; }
+  DeviceArray<ValueType>& values() { return v_; }
+  const DeviceArray<int32_t>& crow_offsets() const { return ro_; }
+  const DeviceArray<int32_t>& ccolumn_indices() const { return ci_; }
+  const DeviceArray<ValueType>& cvalues() const { return v_; }
+  mgb_csr desc() const {
+    return mgb_csr{nrows_, ncols_, nnz_, const_cast<int32_t*>(ro_.data()), const_cast<int32_t*>(ci_.data()),
+                   const_cast<ValueType*>(v_.data())};
+  }
+
+ private:
+  int64_t nrows_ = 0, ncols_ = 0, nnz_ = 0;
+  DeviceArray<int32_t> ro_, ci_;
+  DeviceArray<ValueType> v_;
+};
+
+template <class ValueType>
+class DiaMatrix {  // core/src/Morpheus_DiaMatrix.hpp:192-201, values (pad(N,32) x ndiags) column-major
+ public:
+  using value_type = ValueType;
+  static constexpr formats_e format = DIA_FORMAT;
+  DiaMatrix() = default;
+  DiaMatrix(int64_t r, int64_t c, int64_t n, int64_t nd, int64_t align = 32) { resize(r, c, n, nd, align); }
+  DiaMatrix(int64_t r, int64_t c, int64_t n, const std::vector<int32_t>& offs,
+            const std::vector<ValueType>& vals, int64_t align = 32)
+      : nrows_(r), ncols_(c), nnz_(n), ndiags_((int64_t)offs.size()), align_(align),
+        pitch_(Impl::get_pad_size(r, align)), off_(offs), v_(vals) {
+    if ((int64_t)vals.size() != pitch_ * ndiags_) throw InvalidInputException("DIA values size");
+  }
+  void resize(int64_t r, int64_t c, int64_t n, int64_t nd, int64_t align = 32) {
+    nrows_ = r; ncols_ = c; nnz_ = n; ndiags_ = nd; align_ = align;
+    pitch_ = Impl::get_pad_size(r, align);
+    off_.resize(nd); v_.resize(pitch_ * nd);
+  }
+  int64_t nrows() const { return nrows_; }
+  int64_t ncols() const { return ncols_; }
+  int64_t nnnz() const { return nnz_; }
+  int64_t ndiags() const { return ndiags_; }
+  int64_t alignment() const { return align_; }
+  int64_t pitch() const { return pitch_; }
+  formats_e format_enum() const { return format; }
+  int format_index() const { return format; }
+  DeviceArray<int32_t>& diagonal_offsets() { return off_; }
+  DeviceArray<ValueType>& values() { return v_; }
+  const DeviceArray<int32_t>& cdiagonal_offsets() const { return off_; }
+  const DeviceArray<ValueType>& cvalues() const { return v_; }
+  mgb_dia desc() const {
+    return mgb_dia{nrows_, ncols_, nnz_, ndiags_, pitch_, const_cast<int32_t*>(off_.data()),
+                   const_cast<ValueType*>(v_.data())};
+  }
+
+ private:
+  int64_t nrows_ = 0, ncols_ = 0, nnz_ = 0, ndiags_ = 0, align_ = 32, pitch_ = 0;
+  DeviceArray<int32_t> off_;
+  DeviceArray<ValueType> v_;
+};
+
+template <class ValueType>
+class EllMatrix {  // core/src/Morpheus_EllMatrix.hpp:189-202; slots (N x pad(W,32)) column-major
+ public:
+  using value_type = ValueType;
+  static constexpr formats_e format = ELL_FORMAT;
+  static constexpr int32_t invalid_index() { return MGB_INVALID_INDEX; }
+  EllMatrix() = default;
+  EllMatrix(int64_t r, int64_t c, int64_t n, int64_t epr, int64_t align = 32) { resize(r, c, n, epr, align); }
+  EllMatrix(int64_t r, int64_t c, int64_t n, int64_t epr, const std::vector<int32_t>& ci,
+            const std::vector<ValueType>& v, int64_t align = 32)
+      : nrows_(r), ncols_(c), nnz_(n), epr_(epr), align_(align), width_(Impl::get_pad_size(epr, align)),
+        ci_(ci), v_(v) {
+    if ((int64_t)ci.size() != r * width_ || ci.size() != v.size()) throw InvalidInputException("ELL sizes");
+  }
+  void resize(int64_t r, int64_t c, int64_t n, int64_t epr, int64_t align = 32) {
+    nrows_ = r; ncols_ = c; nnz_ = n; epr_ = epr; align_ = align;
+    width_ = Impl::get_pad_size(epr, align);
+    ci_.resize(r * width_, MGB_INVALID_INDEX);
+    v_.resize(r * width_);
+  }
+  int64_t nrows() const { return nrows_; }
+  int64_t ncols() const { return ncols_; }
+  int64_t nnnz() const { return nnz_; }
+  int64_t entries_per_row() const { return epr_; }
+  int64_t alignment() const { return align_; }
+  formats_e format_enum() const { return format; }
+  int format_index() const { return format; }
+  DeviceArray<int32_t>& column_indices() { return ci_; }
+  DeviceArray<ValueType>& values() { return v_; }
+  const DeviceArray<int32_t>& ccolumn_indices() const { return ci_; }
+  const DeviceArray<ValueType>& cvalues() const { return v_; }
+  mgb_ell desc() const {
+    return mgb_ell{nrows_, ncols_, nnz_, epr_, width_, nrows_, const_cast<int32_t*>(ci_.data()),
+                   const_cast<ValueType*>(v_.data())};
+  }
+
+ private:
+  int64_t nrows_ = 0, ncols_ = 0, nnz_ = 0, epr_ = 0, align_ = 32, width_ = 0;
+  DeviceArray<int32_t> ci_;
+  DeviceArray<ValueType> v_;
+};
+
+template <class ValueType>
+class HybMatrix {  // core/src/Morpheus_HybMatrix.hpp:473-476
+ public:
+  using value_type = ValueType;
+  static constexpr formats_e format = HYB_FORMAT;
+  HybMatrix() = default;
+  HybMatrix(EllMatrix<ValueType> e, CooMatrix<ValueType> c) : ell_(std::move(e)), coo_(std::move(c)) {}
+  int64_t nrows() const { return ell_.nrows(); }
+  int64_t ncols() const { return ell_.ncols(); }
+  int64_t nnnz() const { return ell_.nnnz() + coo_.nnnz(); }
+  formats_e format_enum() const { return format; }
+  int format_index() const { return format; }
+  EllMatrix<ValueType>& ell() { return ell_; }
+  CooMatrix<ValueType>& coo() { return coo_; }
+  const EllMatrix<ValueType>& cell() const { return ell_; }
+  const CooMatrix<ValueType>& ccoo() const { return coo_; }
+  mgb_hyb desc() const { return mgb_hyb{ell_.desc(), coo_.desc()}; }
+
+ private:
+  EllMatrix<ValueType> ell_;
+  CooMatrix<ValueType> coo_;
+};
+
+template <class ValueType>
+class HdcMatrix {  // core/src/Morpheus_HdcMatrix.hpp:464-467
+ public:
+  using value_type = ValueType;
+  static constexpr formats_e format = HDC_FORMAT;
+  static constexpr double true_diagonal_ratio = 0.2;
+  HdcMatrix() = default;
+  HdcMatrix(DiaMatrix<ValueType> d, CsrMatrix<ValueType> c) : dia_(std::move(d)), csr_(std::move(c)) {}
+  int64_t nrows() const { return dia_.nrows(); }
+  int64_t ncols() const { return dia_.ncols(); }
+  int64_t nnnz() const { return dia_.nnnz() + csr_.nnnz(); }
+  formats_e format_enum() const { return format; }
+  int format_index() const { return format; }
+  DiaMatrix<ValueType>& dia() { return dia_; }
+  CsrMatrix<ValueType>& csr() { return csr_; }
+  const DiaMatrix<ValueType>& cdia() const { return dia_; }
+  const CsrMatrix<ValueType>& ccsr() const { return csr_; }
+  mgb_hdc desc() const { return mgb_hdc{dia_.desc(), csr_.desc()}; }
+
+ private:
+  DiaMatrix<ValueType> dia_;
+  CsrMatrix<ValueType> csr_;
+};
+
+// ---------------------------------------------------------- DynamicMatrix ---
+// core/src/Morpheus_DynamicMatrix.hpp:102-462
+template <class ValueType>
+class DynamicMatrix {
+ public:
+  using value_type = ValueType;
+  using variant_type = std::variant<CooMatrix<ValueType>, CsrMatrix<ValueType>, DiaMatrix<ValueType>,
+                                    EllMatrix<ValueType>, HybMatrix<ValueType>, HdcMatrix<ValueType>>;
+  DynamicMatrix() = default;
+  template <class M>
+  DynamicMatrix(M m) : v_(std::move(m)) {}
+  template <class M>
+  DynamicMatrix& operator=(M m) {
+    v_ = std::move(m);
+    return *this;
+  }
+  int active_index() const { return (int)v_.index(); }
+  formats_e active_enum() const { return (formats_e)v_.index(); }
+  // Switches to an EMPTY container of the new format (no data is converted);
+  // an index past the last format leaves the matrix unchanged
+  // (core/src/Morpheus_DynamicMatrix.hpp:409-442).
+  void activate(int idx) {
+    switch (idx) {
+      case COO_FORMAT: v_ = CooMatrix<ValueType>(); break;
+      case CSR_FORMAT: v_ = CsrMatrix<ValueType>(); break;
+      case DIA_FORMAT: v_ = DiaMatrix<ValueType>(); break;
+      case ELL_FORMAT: v_ = EllMatrix<ValueType>(); break;
+      case HYB_FORMAT: v_ = HybMatrix<ValueType>(); break;
+      case HDC_FORMAT: v_ = HdcMatrix<ValueType>(); break;
+      default: break;
+    }
+  }
+  void activate(formats_e f) { activate((int)f); }
+  int64_t nrows() const { return std::visit([](const auto& m) { return m.nrows(); }, v_); }
+  int64_t ncols() const { return std::visit([](const auto& m) { return m.ncols(); }, v_); }
+  int64_t nnnz() const { return std::visit([](const auto& m) { return m.nnnz(); }, v_); }
+  variant_type& formats() { return v_; }
+  const variant_type& const_formats() const { return v_; }
+
+ private:
+  variant_type v_;
+};
+
+// ----------------------------------------------------------- algorithms ---
+namespace Impl {
+template <class ExecSpace>
+constexpr void require_gb300() {
+  static_assert(std::is_same_v<typename ExecSpace::execution_space, GB300>,
+                "Morpheus_GB300.hpp implements the GB300 execution space only");
+}
+template <class T> struct Suffix;
+template <> struct Suffix<double> {
+  static int csr(const mgb_csr* a, const double* x, double* y, int i, void* s) { return mgb_spmv_csr_f64(a, x, y, i, s); }
+  static int coo(const mgb_coo* a, const double* x, double* y, int i, void* s) { return mgb_spmv_coo_f64(a, x, y, i, s); }
+  static int dia(const mgb_dia* a, const double* x, double* y, int i, void* s) { return mgb_spmv_dia_f64(a, x, y, i, s); }
+  static int ell(const mgb_ell* a, const double* x, double* y, int i, void* s) { return mgb_spmv_ell_f64(a, x, y, i, s); }
+  static int hyb(const mgb_hyb* a, const double* x, double* y, int i, void* s) { return mgb_spmv_hyb_f64(a, x, y, i, s); }
+  static int hdc(const mgb_hdc* a, const double* x, double* y, int i, void* s) { return mgb_spmv_hdc_f64(a, x, y, i, s); }
+  static int dot(int64_t n, const double* x, const double* y, double* r) { return mgb_dot_f64(n, x, y, r, nullptr); }
+  static int reduce(const double* x, int64_t n, double* r) { return mgb_reduce_f64(x, n, r, nullptr); }
+  static int waxpby(int64_t n, double a, const double* x, double b, const double* y, double* w) {
+    return mgb_waxpby_f64(n, a, x, b, y, w, nullptr);
+  }
+};
+template <> struct Suffix<float> {
+  static int csr(const mgb_csr* a, const float* x, float* y, int i, void* s) { return mgb_spmv_csr_f32(a, x, y, i, s); }
+  static int coo(const mgb_coo* a, const float* x, float* y, int i, void* s) { return mgb_spmv_coo_f32(a, x, y, i, s); }
+  static int dia(const mgb_dia* a, const float* x, float* y, int i, void* s) { return mgb_spmv_dia_f32(a, x, y, i, s); }
+  static int ell(const mgb_ell* a, const float* x, float* y, int i, void* s) { return mgb_spmv_ell_f32(a, x, y, i, s); }
+  static int hyb(const mgb_hyb* a, const float* x, float* y, int i, void* s) { return mgb_spmv_hyb_f32(a, x, y, i, s); }
+  static int hdc(const mgb_hdc* a, const float* x, float* y, int i, void* s) { return mgb_spmv_hdc_f32(a, x, y, i, s); }
+  static int dot(int64_t n, const float* x, const float* y, float* r) { return mgb_dot_f32(n, x, y, r, nullptr); }
+  static int reduce(const float* x, int64_t n, float* r) { return mgb_reduce_f32(x, n, r, nullptr); }
+  static int waxpby(int64_t n, float a, const float* x, float b, const float* y, float* w) {
+    return mgb_waxpby_f32(n, a, x, b, y, w, nullptr);
+  }
+};
+
+template <class T>
+void spmv(const CsrMatrix<T>& A, const T* x, T* y, bool init) {
+  auto d = A.desc();
+  check(Suffix<T>::csr(&d, x, y, init, nullptr), "multiply<GB300>(CsrMatrix)");
+}
+template <class T>
+void spmv(const CooMatrix<T>& A, const T* x, T* y, bool init) {
+  auto d = A.desc();
+  check(Suffix<T>::coo(&d, x, y, init, nullptr), "multiply<GB300>(CooMatrix)");
+}
+template <class T>
+void spmv(const DiaMatrix<T>& A, const T* x, T* y, bool init) {
+  auto d = A.desc();
+  check(Suffix<T>::dia(&d, x, y, init, nullptr), "multiply<GB300>(DiaMatrix)");
+}
+template <class T>
+void spmv(const EllMatrix<T>& A, const T* x, T* y, bool init) {
+  auto d = A.desc();
+  check(Suffix<T>::ell(&d, x, y, init, nullptr), "multiply<GB300>(EllMatrix)");
+}
+template <class T>
+void spmv(const HybMatrix<T>& A, const T* x, T* y, bool init) {
+  auto d = A.desc();
+  check(Suffix<T>::hyb(&d, x, y, init, nullptr), "multiply<GB300>(HybMatrix)");
+}
+template <class T>
+void spmv(const HdcMatrix<T>& A, const T* x, T* y, bool init) {
+  auto d = A.desc();
+  check(Suffix<T>::hdc(&d, x, y, init, nullptr), "multiply<GB300>(HdcMatrix)");
+}
+template <class T>
+void spmv(const DynamicMatrix<T>& A, const T* x, T* y, bool init) {  // impl/Dynamic/Morpheus_Multiply_Impl.hpp:35-44
+  std::visit([&](const auto& m) { spmv(m, x, y, init); }, A.const_formats());
+}
+}  // namespace Impl
+
+// core/src/Morpheus_Multiply.hpp:57-61
+template <class ExecSpace, class Matrix, class Vector>
+inline void multiply(const Matrix& A, const Vector& x, Vector& y, const bool init) {
+  Impl::require_gb300<ExecSpace>();
+  if ((int64_t)x.size() < A.ncols() || (int64_t)y.size() < A.nrows())
+    throw InvalidInputException("multiply: vector sizes do not match the matrix");
+  Impl::spmv(A, x.data(), y.data(), init);
+}
+
+// core/src/Morpheus_Multiply.hpp:75-78
+template <class ExecSpace, class Matrix, class Vector>
+inline void multiply(const Matrix& A, const Vector& x, Vector& y) {
+  multiply<ExecSpace>(A, x, y, true);
+}
+
+// core/src/Morpheus_Dot.hpp:50-58
+template <class ExecSpace, class Vector1, class Vector2>
+inline typename Vector2::value_type dot(size_t n, const Vector1& x, const Vector2& y) {
+  Impl::require_gb300<ExecSpace>();
+  typename Vector2::value_type r{};
+  Impl::check(Impl::Suffix<typename Vector2::value_type>::dot((int64_t)n, x.data(), y.data(), &r), "dot<GB300>");
+  return r;
+}
+
+// core/src/Morpheus_Reduction.hpp:46-52
+template <class ExecSpace, class Vector>
+inline typename Vector::value_type reduce(const Vector& in, size_t size) {
+  Impl::require_gb300<ExecSpace>();
+  typename Vector::value_type r{};
+  Impl::check(Impl::Suffix<typename Vector::value_type>::reduce(in.data(), (int64_t)size, &r), "reduce<GB300>");
+  return r;
+}
+
+// core/src/Morpheus_WAXPBY.hpp:52-64
+template <class ExecSpace, class Vector1, class Vector2, class Vector3>
+inline void waxpby(size_t n, typename Vector1::value_type alpha, const Vector1& x,
+                   typename Vector2::value_type beta, const Vector2& y, Vector3& w) {
+  Impl::require_gb300<ExecSpace>();
+  Impl::check(Impl::Suffix<typename Vector1::value_type>::waxpby((int64_t)n, alpha, x.data(), beta, y.data(),
+                                                                 w.data()),
+              "waxpby<GB300>");
+}
+
+}  // namespace Morpheus
+
+#endif  // MORPHEUS_GB300_HPP

@@ -169,6 +169,69 @@ int mgb_reduce_f32_async(const float* in, int64_t size, float* d_result, void* s
 int mgb_waxpby_f64(int64_t n, double alpha, const double* x, double beta, const double* y, double* w, void* stream);
 int mgb_waxpby_f32(int64_t n, float alpha, const float* x, float beta, const float* y, float* w, void* stream);
 
+/* ---- format conversion on the device ------------------------------------
+ * Morpheus::convert<ExecSpace>(src, dst) (core/src/Morpheus_Convert.hpp:53-57)
+ * for every pair through COO (impl/Morpheus_Convert_Impl.hpp:82-104); the
+ * reference's CUDA space throws NotImplementedException for all of them
+ * (impl/<Fmt>/Cuda/Morpheus_Convert_Impl.hpp), so each entry point below
+ * replaces the Serial routine named beside it and returns bit-identical
+ * structures (indices, padding, order, tie-breaks).
+ *
+ * Destinations are caller-allocated: set every size field of *dst and point
+ * its arrays at device buffers of those sizes.  Sizes that depend on the data
+ * come from the matching *_plan call, which also applies the reference's
+ * fill-tolerance test (impl/Morpheus_Utils.hpp:91-105) and returns
+ * MGB_ERR_FORMAT_CONVERSION where the reference throws
+ * FormatConversionException.  Rows/columns outside the matrix are rejected
+ * with MGB_ERR_INVALID_INPUT (the reference indexes out of bounds there).
+ * Conversions synchronise the stream (they read sizes back to the host). */
+
+/* impl/Csr/Serial/Morpheus_Convert_Impl.hpp:70-97; dst: nnz entries */
+int mgb_convert_csr_to_coo_f64(const mgb_csr* src, mgb_coo* dst, void* stream);
+int mgb_convert_csr_to_coo_f32(const mgb_csr* src, mgb_coo* dst, void* stream);
+/* impl/Csr/Serial/Morpheus_Convert_Impl.hpp:99-151; dst: nrows+1 offsets, nnz entries */
+int mgb_convert_coo_to_csr_f64(const mgb_coo* src, mgb_csr* dst, void* stream);
+int mgb_convert_coo_to_csr_f32(const mgb_coo* src, mgb_csr* dst, void* stream);
+/* impl/Dia/Serial/Morpheus_Convert_Impl.hpp:72-118; dst: src->nnz entries */
+int mgb_convert_dia_to_coo_f64(const mgb_dia* src, mgb_coo* dst, void* stream);
+int mgb_convert_dia_to_coo_f32(const mgb_dia* src, mgb_coo* dst, void* stream);
+/* impl/Dia/Serial/Morpheus_Convert_Impl.hpp:120-169 */
+int mgb_convert_coo_to_dia_plan(const mgb_coo* src, int64_t* ndiags, void* stream);
+int mgb_convert_coo_to_dia_f64(const mgb_coo* src, mgb_dia* dst, void* stream);
+int mgb_convert_coo_to_dia_f32(const mgb_coo* src, mgb_dia* dst, void* stream);
+/* impl/Ell/Serial/Morpheus_Convert_Impl.hpp:68-109 */
+int mgb_convert_ell_to_coo_f64(const mgb_ell* src, mgb_coo* dst, void* stream);
+int mgb_convert_ell_to_coo_f32(const mgb_ell* src, mgb_coo* dst, void* stream);
+/* impl/Ell/Serial/Morpheus_Convert_Impl.hpp:111-173 (width = longest row) */
+int mgb_convert_coo_to_ell_plan(const mgb_coo* src, int64_t* entries_per_row, void* stream);
+int mgb_convert_coo_to_ell_f64(const mgb_coo* src, mgb_ell* dst, void* stream);
+int mgb_convert_coo_to_ell_f32(const mgb_coo* src, mgb_ell* dst, void* stream);
+/* impl/Hyb/Serial/Morpheus_Convert_Impl.hpp:62-108 */
+int mgb_convert_hyb_to_coo_f64(const mgb_hyb* src, mgb_coo* dst, void* stream);
+int mgb_convert_hyb_to_coo_f32(const mgb_hyb* src, mgb_coo* dst, void* stream);
+/* impl/Hyb/Serial/Morpheus_Convert_Impl.hpp:110-196.  width = 0 selects the
+ * reference rule max(1, nnz / nrows); the fill call reads the width from
+ * dst->ell.entries_per_row. */
+int mgb_convert_coo_to_hyb_plan(const mgb_coo* src, int64_t width, int64_t* entries_per_row, int64_t* ell_nnz,
+                                int64_t* coo_nnz, void* stream);
+int mgb_convert_coo_to_hyb_f64(const mgb_coo* src, mgb_hyb* dst, void* stream);
+int mgb_convert_coo_to_hyb_f32(const mgb_coo* src, mgb_hyb* dst, void* stream);
+/* impl/Hdc/Serial/Morpheus_Convert_Impl.hpp:64-130 */
+int mgb_convert_hdc_to_coo_f64(const mgb_hdc* src, mgb_coo* dst, void* stream);
+int mgb_convert_hdc_to_coo_f32(const mgb_hdc* src, mgb_coo* dst, void* stream);
+/* impl/Hdc/Serial/Morpheus_Convert_Impl.hpp:132-226 (true diagonals hold at
+ * least floor(0.2 * nrows) entries) */
+int mgb_convert_coo_to_hdc_plan(const mgb_coo* src, int64_t* ndiags, int64_t* dia_nnz, int64_t* csr_nnz,
+                                void* stream);
+int mgb_convert_coo_to_hdc_f64(const mgb_coo* src, mgb_hdc* dst, void* stream);
+int mgb_convert_coo_to_hdc_f32(const mgb_coo* src, mgb_hdc* dst, void* stream);
+
+/* In-place stable sort by (row, column): impl/Coo/Serial/Morpheus_Sort_Impl.hpp:109-164 */
+int mgb_coo_sort_by_row_and_column_f64(mgb_coo* A, void* stream);
+int mgb_coo_sort_by_row_and_column_f32(mgb_coo* A, void* stream);
+/* impl/Coo/Serial/Morpheus_Sort_Impl.hpp:166-186; *sorted = 1 or 0 */
+int mgb_coo_is_sorted(const mgb_coo* A, int* sorted, void* stream);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif

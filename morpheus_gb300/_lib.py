@@ -66,6 +66,20 @@ for _dt, _ct in (("f64", C.c_double), ("f32", C.c_float)):
     _SIGS[f"mgb_reduce_{_dt}"] = (C.c_int, [vp, i64, C.POINTER(_ct), vp])
     _SIGS[f"mgb_reduce_{_dt}_async"] = (C.c_int, [vp, i64, vp, vp])
     _SIGS[f"mgb_waxpby_{_dt}"] = (C.c_int, [i64, _ct, vp, _ct, vp, vp, vp])
+_P = C.POINTER
+for _name, _s, _d in (("csr_to_coo", Csr, Coo), ("coo_to_csr", Coo, Csr), ("dia_to_coo", Dia, Coo),
+                      ("coo_to_dia", Coo, Dia), ("ell_to_coo", Ell, Coo), ("coo_to_ell", Coo, Ell),
+                      ("hyb_to_coo", Hyb, Coo), ("coo_to_hyb", Coo, Hyb), ("hdc_to_coo", Hdc, Coo),
+                      ("coo_to_hdc", Coo, Hdc)):
+    for _dt in ("f64", "f32"):
+        _SIGS[f"mgb_convert_{_name}_{_dt}"] = (C.c_int, [_P(_s), _P(_d), vp])
+_SIGS["mgb_convert_coo_to_dia_plan"] = (C.c_int, [_P(Coo), _P(i64), vp])
+_SIGS["mgb_convert_coo_to_ell_plan"] = (C.c_int, [_P(Coo), _P(i64), vp])
+_SIGS["mgb_convert_coo_to_hyb_plan"] = (C.c_int, [_P(Coo), i64, _P(i64), _P(i64), _P(i64), vp])
+_SIGS["mgb_convert_coo_to_hdc_plan"] = (C.c_int, [_P(Coo), _P(i64), _P(i64), _P(i64), vp])
+for _dt in ("f64", "f32"):
+    _SIGS[f"mgb_coo_sort_by_row_and_column_{_dt}"] = (C.c_int, [_P(Coo), vp])
+_SIGS["mgb_coo_is_sorted"] = (C.c_int, [_P(Coo), _P(C.c_int), vp])
 
 
 def load(path: str | None = None):

@@ -176,12 +176,14 @@ spmv_csr_segments(int64_t nrows, int64_t ncols, int64_t nnz, int64_t nchunks,
         if (r < r_end) {
           rs = re;
           re = ro_at(r + 1);
-          acc = init ? T(0) : y[r];
+          acc = init ? T(0) : y[r];  // empty rows at lb are flushed here
         }
       }
     }
-    // tail partial (row continuing into the next lane) and segmented scan
-    const bool has_tail = active && r < r_end;
+    // tail partial (a row that started in this lane's range and continues into
+    // the next lane; a row starting exactly at lb belongs to the next lane)
+    // and segmented scan
+    const bool has_tail = active && r < r_end && rs < lb;
     const int64_t key = has_tail ? r : -1 - (int64_t)lane;
     T cv = has_tail ? acc : T(0);
 #pragma unroll
