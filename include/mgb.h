@@ -126,6 +126,19 @@ int mgb_spmv_csr_f32(const mgb_csr* A, const float* x, float* y, int init, void*
 int mgb_spmv_coo_f64(const mgb_coo* A, const double* x, double* y, int init, void* stream);
 int mgb_spmv_coo_f32(const mgb_coo* A, const float* x, float* y, int init, void* stream);
 
+/* Allocation-free variant of mgb_spmv_coo_f64; it has no counterpart in the
+ * reference.  For callers that may not allocate device memory while they run
+ * (code inside an allocation-free graph-capture region, hosts that reserve all
+ * device memory up front, plugins whose host owns the allocator): the carry
+ * buffer is a fixed 4 MiB file-scope device array instead of cudaMallocAsync,
+ * and no allocating call is made.  Limits: A->nnz <= 44,736,512, otherwise
+ * MGB_ERR_INVALID_INPUT before any work is queued; every GPU that loads the
+ * library holds the 4 MiB until exit; the first call on a device looks up the
+ * array's address (make it before any stream capture); all calls share the
+ * array, so calls overlapping on the GPU race -- serialise them.  Same result
+ * as mgb_spmv_coo_f64. */
+int mgb_spmv_coo_f64_noalloc(const mgb_coo* A, const double* x, double* y, int init, void* stream);
+
 /* replaces impl/Dia/Cuda/Morpheus_Multiply_Impl.hpp:41-85 */
 int mgb_spmv_dia_f64(const mgb_dia* A, const double* x, double* y, int init, void* stream);
 int mgb_spmv_dia_f32(const mgb_dia* A, const float* x, float* y, int init, void* stream);

@@ -66,6 +66,7 @@ for _dt, _ct in (("f64", C.c_double), ("f32", C.c_float)):
     _SIGS[f"mgb_reduce_{_dt}"] = (C.c_int, [vp, i64, C.POINTER(_ct), vp])
     _SIGS[f"mgb_reduce_{_dt}_async"] = (C.c_int, [vp, i64, vp, vp])
     _SIGS[f"mgb_waxpby_{_dt}"] = (C.c_int, [i64, _ct, vp, _ct, vp, vp, vp])
+_SIGS["mgb_spmv_coo_f64_noalloc"] = (C.c_int, [C.POINTER(Coo), vp, vp, C.c_int, vp])
 _P = C.POINTER
 for _name, _s, _d in (("csr_to_coo", Csr, Coo), ("coo_to_csr", Coo, Csr), ("dia_to_coo", Dia, Coo),
                       ("coo_to_dia", Coo, Dia), ("ell_to_coo", Ell, Coo), ("coo_to_ell", Coo, Ell),

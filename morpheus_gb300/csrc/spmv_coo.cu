@@ -236,3 +236,98 @@ int mgb_spmv_coo_f32(const mgb_coo* A, const float* x, float* y, int init, void*
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free COO SpMV.
+//
+// For callers that cannot allocate device memory while they run: code inside
+// a CUDA-graph-captured region of a host application that forbids
+// allocations, real-time or embedded hosts that reserve all memory up front,
+// and plugins whose host process owns the allocator.  mgb_spmv_coo_f64 takes
+// its carry buffer from cudaMallocAsync; this variant takes it from a fixed
+// file-scope device array instead, so it never calls cudaMalloc, cudaFree or
+// any allocating routine.
+//
+// Limits and rules:
+//  * The array is COO_NOALLOC_BYTES (4 MiB) of device memory that every GPU
+//    which loads this library holds until the process exits.  It holds two
+//    carries (int32 row + double value) per 256-entry chunk, so A->nnz may be
+//    at most 44,736,512; larger matrices get MGB_ERR_INVALID_INPUT before any
+//    work is queued.
+//  * The first call on a device looks up the array's device address with
+//    cudaGetSymbolAddress (once per device, with that device current) and
+//    caches it; make that first call before any stream capture.
+//  * Every call uses the same array and leaves the previous call's carries
+//    in it.  Nothing in it needs to start at zero: each call writes every
+//    carry slot it reads.  Calls that overlap on the GPU (other streams, other
+//    host threads) race on the array; serialise them.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+namespace mgb {
+namespace {
+constexpr size_t COO_NOALLOC_BYTES = size_t(4) << 20;
+}  // namespace
+}  // namespace mgb
+
+static __device__ __align__(256) unsigned char g_coo_noalloc_scratch[mgb::COO_NOALLOC_BYTES];
+
+namespace mgb {
+namespace {
+
+std::mutex g_noalloc_mutex;
+void* g_noalloc_ptr[128] = {};
+
+// Device address of the scratch array for the current device (set-up on the
+// first call per device).
+int noalloc_scratch(void** out) {
+  int dev = 0;
+  MGB_CUDA_CHECK(cudaGetDevice(&dev));
+  MGB_REQUIRE(dev >= 0 && dev < 128, MGB_ERR_RUNTIME);
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (g_noalloc_ptr[dev] == nullptr) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_coo_noalloc_scratch);
+    if (e != cudaSuccess) return record_cuda_error(e);
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return MGB_SUCCESS;
+}
+
+int launch_coo_noalloc_f64(const mgb_coo* A, const double* x, double* y, int init, cudaStream_t s) {
+  MGB_REQUIRE(A != nullptr, MGB_ERR_BAD_ARGUMENT);
+  MGB_REQUIRE(!bad_sizes(A->nrows, A->ncols, A->nnz), MGB_ERR_BAD_ARGUMENT);
+  const int64_t nchunks = (A->nnz + COO_CH - 1) / COO_CH;
+  const int64_t ncarry = 2 * nchunks;
+  const size_t rows_bytes = ((sizeof(int32_t) * (size_t)ncarry + 255) / 256) * 256;
+  MGB_REQUIRE(rows_bytes + sizeof(double) * (size_t)ncarry <= COO_NOALLOC_BYTES, MGB_ERR_INVALID_INPUT);
+  MGB_REQUIRE(A->nrows < ((int64_t)1 << 31), MGB_ERR_INVALID_INPUT);
+  if (A->nrows == 0) return MGB_SUCCESS;
+  MGB_REQUIRE(y != nullptr, MGB_ERR_BAD_ARGUMENT);
+  if (A->nnz == 0) {
+    if (init) MGB_CUDA_CHECK(cudaMemsetAsync(y, 0, sizeof(double) * A->nrows, s));
+    return MGB_SUCCESS;
+  }
+  MGB_REQUIRE(A->row_indices && A->column_indices && A->values && x, MGB_ERR_BAD_ARGUMENT);
+  void* scratch = nullptr;
+  int st = noalloc_scratch(&scratch);
+  if (st != MGB_SUCCESS) return st;
+  int32_t* cr = static_cast<int32_t*>(scratch);
+  double* cv = reinterpret_cast<double*>(static_cast<char*>(scratch) + rows_bytes);
+  const int64_t blocks = (nchunks + COO_WARPS - 1) / COO_WARPS;
+  spmv_coo_chunks<double><<<(unsigned)blocks, COO_WARPS * 32, 0, s>>>(
+      A->nrows, A->ncols, A->nnz, A->row_indices, A->column_indices,
+      static_cast<const double*>(A->values), x, y, init, cr, cv);
+  MGB_LAUNCH_CHECK();
+  coo_carry_fixup<double><<<(unsigned)((ncarry + 255) / 256), 256, 0, s>>>(ncarry, A->nrows, cr, cv, y, init);
+  MGB_LAUNCH_CHECK();
+  return MGB_SUCCESS;
+}
+
+}  // namespace
+}  // namespace mgb
+
+extern "C" int mgb_spmv_coo_f64_noalloc(const mgb_coo* A, const double* x, double* y, int init, void* stream) {
+  return mgb::launch_coo_noalloc_f64(A, x, y, init, mgb::as_stream(stream));
+}
