@@ -185,21 +185,41 @@ def run_reference(args, rank: int):
     if rank != 0:
         return
     dtype = np.float64 if args.dtype == "f64" else np.float32
-    A, hm = build_workload(args.workload, args.format, dtype, seed=0)
     vbytes = np.dtype(dtype).itemsize
-    nbytes = algorithmic_bytes(hm, vbytes)
-    x = np.random.default_rng(1).uniform(-1, 1, hm["ncols"]).astype(dtype)
     from oracle import oracle as O
     from oracle.build import build_oracle
     build_oracle()
     threads = O.max_threads()
-    om = O.OracleMatrix.from_host(hm)
-    y = np.zeros(hm["nrows"], dtype=dtype)
+    if args.workload == "batched":
+        from morpheus_gb300 import generators as gen
+        mats = gen.batched_csr(args.batch, seed=0, dtype=dtype)
+        sample = mats[: min(len(mats), 256)]  # bounded sample per step
+        oms = [O.OracleMatrix.from_host(m) for m in sample]
+        xs = [np.random.default_rng(1 + i).uniform(-1, 1, m["ncols"]).astype(dtype) for i, m in enumerate(sample)]
+        ysb = [np.zeros(m["nrows"], dtype=dtype) for m in sample]
+        nbytes = sum(algorithmic_bytes(m, vbytes) for m in sample)
+
+        def step():
+            for om, xv, yv in zip(oms, xs, ysb):
+                om.multiply(xv, yv, init=True, threads=threads)
+        hm = {"nrows": sum(m["nrows"] for m in mats), "ncols": sum(m["ncols"] for m in mats),
+              "nnz": sum(m["nnz"] for m in mats)}
+        sample_desc = f"first {len(sample)} of {len(mats)} matrices per step, one OpenMP multiply each"
+    else:
+        A, hm = build_workload(args.workload, args.format, dtype, seed=0)
+        nbytes = algorithmic_bytes(hm, vbytes)
+        x = np.random.default_rng(1).uniform(-1, 1, hm["ncols"]).astype(dtype)
+        om = O.OracleMatrix.from_host(hm)
+        y = np.zeros(hm["nrows"], dtype=dtype)
+
+        def step():
+            om.multiply(x, y, init=True, threads=threads)
+        sample_desc = f"full matrix, {args.steps} timed multiplies"
     for _ in range(args.warmup):
-        om.multiply(x, y, init=True, threads=threads)
+        step()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        om.multiply(x, y, init=True, threads=threads)
+        step()
     el = time.perf_counter() - t0
     gbs = nbytes * args.steps / el / 1e9
     line = {
@@ -208,8 +228,7 @@ def run_reference(args, rank: int):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": args.dtype,
         "data": "synthetic (seeded)", "config": config_dict(args, hm),
         "cpu_baseline": {"value": gbs, "unit": "GB/s", "cores": threads, "kind": "port",
-                         "sample": f"full matrix, {args.steps} timed multiplies (reference OpenMP "
-                                   f"algorithm restated in oracle/oracle.cpp)"},
+                         "sample": f"{sample_desc} (reference OpenMP algorithm restated in oracle/oracle.cpp)"},
         "e2e": {"value": gbs, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -219,7 +238,9 @@ METRIC = "SpMV GB/s (% HBM peak)"
 
 
 def config_dict(args, hm):
-    return {"workload": f"{args.workload}_{args.format}_{args.dtype}", "format": args.format.upper(),
+    name = (f"batched_csr_{args.batch}_{args.dtype}" if args.workload == "batched"
+            else f"{args.workload}_{args.format}_{args.dtype}")
+    return {"workload": name, "format": args.format.upper(),
             "nrows": hm["nrows"], "ncols": hm["ncols"], "nnz": hm["nnz"],
             "l2": "inputs larger than L2 (no flush needed)" if args.workload != "laplacian"
             else "L2 flushed between steps (256 MB scratch write)",
@@ -392,6 +413,141 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
     print(json.dumps(line), flush=True)
 
 
+def run_gpu_batched(args, rank: int, world: int, local_rank: int):
+    """4,096 independent FP64 CSR SpMVs per step in one autotuned persistent
+    launch, replayed as a CUDA graph; baseline: the same SpMVs as separate
+    single-matrix calls."""
+    import torch
+
+    import morpheus_gb300 as mgb
+    from morpheus_gb300 import batched
+    from morpheus_gb300 import generators as gen
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    dtype = np.float64 if args.dtype == "f64" else np.float32
+    vbytes = np.dtype(dtype).itemsize
+    mats = gen.batched_csr(args.batch, seed=rank, dtype=dtype)
+    nbytes = sum(algorithmic_bytes(m, vbytes) for m in mats)
+    dmats = [mgb.matrix_from_host(m, device=dev) for m in mats]
+    xs_np = [np.random.default_rng(1 + i).uniform(-1, 1, m["ncols"]).astype(dtype) for i, m in enumerate(mats)]
+    xs = [torch.from_numpy(v).to(dev) for v in xs_np]
+    ys = [torch.zeros(m["nrows"], dtype=dmats[0].dtype, device=dev) for m in mats]
+    b = batched.CsrBatch(dmats, xs, ys)
+    best, tune_ms = b.autotune(reps=3, use_cache=False)
+    check_err = None
+    if rank == 0 and not args.skip_check:
+        from oracle import oracle as O
+        from oracle.build import build_oracle
+        build_oracle()
+        b.multiply()
+        torch.cuda.synchronize()
+        errs = []
+        for i in range(0, len(mats), max(1, len(mats) // 64)):  # 64 sampled matrices
+            ref = O.OracleMatrix.from_host(mats[i]).multiply(xs_np[i])
+            errs.append(np.linalg.norm(ys[i].cpu().numpy() - ref) / max(np.linalg.norm(ref), 1e-300))
+        check_err = float(max(errs))
+    g = b.capture_graph(init=True)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(args.warmup):
+        g.replay()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    time.sleep(0.3)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        g.replay()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    clocks = sampler.stop()
+    kernel_ms = ms / args.steps
+    # baseline: one single-matrix call per matrix (the reference's usage)
+    s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for A, x, y in zip(dmats, xs, ys):
+        mgb.multiply(A, x, y)
+    torch.cuda.synchronize()
+    s0.record(stream)
+    for A, x, y in zip(dmats, xs, ys):
+        mgb.multiply(A, x, y)
+    s1.record(stream)
+    torch.cuda.synchronize()
+    sep_ms = s0.elapsed_time(s1)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * nbytes * args.steps / (ms * 1e-3) / 1e9
+    # e2e: host arrays -> device, batched launch, y -> host, every step
+    host = []
+    for m, xv in zip(mats, xs_np):
+        host.append([torch.from_numpy(np.ascontiguousarray(m[k])).pin_memory()
+                     for k in ("row_offsets", "column_indices", "values")] + [torch.from_numpy(xv).pin_memory()])
+    dsts = [[A.row_offsets(), A.column_indices(), A.values(), x] for A, x in zip(dmats, xs)]
+    yh = [torch.empty(y.numel(), dtype=y.dtype).pin_memory() for y in ys]
+    h2d = sum(t.numel() * t.element_size() for h in host for t in h)
+    d2h = sum(t.numel() * t.element_size() for t in yh)
+    e2e_steps = max(1, min(args.steps, args.e2e_steps))
+    torch.cuda.synchronize()
+    a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a0.record(stream)
+    for _ in range(e2e_steps):
+        for hs, ds in zip(host, dsts):
+            for h, d in zip(hs, ds):
+                d.copy_(h, non_blocking=True)
+        b.multiply()
+        for y, h in zip(ys, yh):
+            h.copy_(y, non_blocking=True)
+    a1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = a0.elapsed_time(a1) / e2e_steps
+    if rank != 0:
+        return
+    peak, peak_src = peaks()
+    achieved = nbytes / (kernel_ms * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": args.dtype, "data": "synthetic (seeded batched CSR generator)",
+        "config": {"workload": f"batched_csr_{args.batch}_{args.dtype}", "matrices": len(mats),
+                   "nnz_total": int(sum(m["nnz"] for m in mats)),
+                   "rows_total": int(sum(m["nrows"] for m in mats)),
+                   "l2": "inputs larger than L2 (no flush needed)", "parallelism": f"replicas x{world}",
+                   "autotuned_config": best, "config_chunk_seg": batched.config_info(best),
+                   "autotune_ms_per_config": tune_ms},
+        "pct_hbm_peak": 100.0 * achieved / peak, "rel_err_vs_oracle": check_err,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "peak_source": peak_src, "algorithmic_bytes_per_launch": nbytes},
+        "separate_calls": {"ms": sep_ms, "GB/s": nbytes / (sep_ms * 1e-3) / 1e9, "launches": 2 * len(mats),
+                           "speedup_of_batched": sep_ms / kernel_ms},
+        "e2e": {"value": world * nbytes / (e2e_ms * 1e-3) / 1e9, "unit": "GB/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
+        "gpu_launches": args.steps * 1, "clocks": clocks,
+    }
+    if not args.no_cpu_baseline:
+        from oracle import oracle as O
+        from oracle.build import build_oracle
+        build_oracle()
+        threads = O.max_threads()
+        oms = [O.OracleMatrix.from_host(m) for m in mats]
+        ys_h = [np.zeros(m["nrows"], dtype=dtype) for m in mats]
+        t0 = time.perf_counter()
+        done_bytes = 0
+        for om, m, xv, yv in zip(oms, mats, xs_np, ys_h):  # the reference: one multiply per matrix
+            om.multiply(xv, yv, init=True, threads=threads)
+            done_bytes += algorithmic_bytes(m, vbytes)
+            if time.perf_counter() - t0 > args.cpu_budget:
+                break
+        el = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": done_bytes / el / 1e9, "unit": "GB/s", "cores": threads, "kind": "port",
+                                "sample": f"one OpenMP multiply per matrix over the batch (reference usage), "
+                                          f"{done_bytes} bytes in {el:.2f} s"}
+    print(json.dumps(line), flush=True)
+
+
 def launches_per_step(hm) -> int:
     f = hm["format"]
     if f == 0:
@@ -421,7 +577,8 @@ def main():
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="mgb", choices=["mgb", "reference"])
-    ap.add_argument("--workload", default="power_law", choices=["power_law", "stencil27", "laplacian"])
+    ap.add_argument("--workload", default="power_law", choices=["power_law", "stencil27", "laplacian", "batched"])
+    ap.add_argument("--batch", type=int, default=4096)
     ap.add_argument("--format", default="csr", choices=["csr", "coo", "dia", "ell", "hyb", "hdc"])
     ap.add_argument("--dtype", default="f64", choices=["f64", "f32"])
     ap.add_argument("--e2e-steps", type=int, default=10)
@@ -439,7 +596,10 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
     try:
-        run_gpu(args, rank, world, local_rank)
+        if args.workload == "batched":
+            run_gpu_batched(args, rank, world, local_rank)
+        else:
+            run_gpu(args, rank, world, local_rank)
     finally:
         if world > 1:
             import torch.distributed as dist

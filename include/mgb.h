@@ -182,6 +182,47 @@ int mgb_reduce_f32_async(const float* in, int64_t size, float* d_result, void* s
 int mgb_waxpby_f64(int64_t n, double alpha, const double* x, double beta, const double* y, double* w, void* stream);
 int mgb_waxpby_f32(int64_t n, float alpha, const float* x, float beta, const float* y, float* w, void* stream);
 
+/* ---- batched CSR SpMV ----------------------------------------------------
+ * No counterpart in the reference, whose equivalent is one
+ * Morpheus::multiply call per matrix (impl/Csr/Cuda/Morpheus_Multiply_Impl.hpp:94-157).
+ * y_i = A_i * x_i (init) or y_i += A_i * x_i for every item, in one persistent
+ * launch: warps take lane-segment chunks of any matrix from an atomic work
+ * counter.  Usage: allocate mgb_spmv_batched_csr_workspace_bytes() of device
+ * memory, plan once per (batch, config) -- the plan reads the device item
+ * array and needs no host synchronisation -- then launch as often as needed.
+ * A launch is a memset of the work counter plus one kernel, so it can be
+ * captured in a CUDA graph.  A launch whose config differs from the planned
+ * one does nothing and sets workspace word 3 to 1.  Items must not share y. */
+typedef struct mgb_csr_batch_item {
+  int64_t nrows, ncols, nnz;
+  int32_t* row_offsets;
+  int32_t* column_indices;
+  void* values;
+  void* x;
+  void* y;
+} mgb_csr_batch_item;
+
+int mgb_spmv_batched_csr_num_configs(void);
+/* chunk = nonzeros per warp chunk, seg = entries staged per lane per step */
+int mgb_spmv_batched_csr_config_info(int config, int64_t* chunk, int* seg);
+int mgb_spmv_batched_csr_workspace_bytes(int64_t nitems, int64_t* bytes);
+int mgb_spmv_batched_csr_plan(const mgb_csr_batch_item* d_items, int64_t nitems, int config, void* workspace,
+                              int64_t workspace_bytes, void* stream);
+int mgb_spmv_batched_csr_f64(const mgb_csr_batch_item* d_items, int64_t nitems, int config, void* workspace,
+                             int init, void* stream);
+int mgb_spmv_batched_csr_f32(const mgb_csr_batch_item* d_items, int64_t nitems, int config, void* workspace,
+                             int init, void* stream);
+/* Autotuner: plans and times every config (`reps` launches each, CUDA
+ * events), writes the fastest to *best_config and the per-config ms to
+ * ms_per_config[num_configs] (may be NULL), and leaves the workspace planned
+ * for the best.  Overwrites every y. Synchronises the stream. */
+int mgb_spmv_batched_csr_autotune_f64(const mgb_csr_batch_item* d_items, int64_t nitems, void* workspace,
+                                      int64_t workspace_bytes, int reps, int* best_config, float* ms_per_config,
+                                      void* stream);
+int mgb_spmv_batched_csr_autotune_f32(const mgb_csr_batch_item* d_items, int64_t nitems, void* workspace,
+                                      int64_t workspace_bytes, int reps, int* best_config, float* ms_per_config,
+                                      void* stream);
+
 /* ---- format conversion on the device ------------------------------------
  * Morpheus::convert<ExecSpace>(src, dst) (core/src/Morpheus_Convert.hpp:53-57)
  * for every pair through COO (impl/Morpheus_Convert_Impl.hpp:82-104); the

@@ -5,6 +5,7 @@ libmorpheus_gb300.so (sm_103a kernels).  See include/mgb.h for the ABI and
 include/Morpheus_GB300.hpp for the C++ front end.
 """
 from .algorithms import dot, dot_async, multiply, reduce, waxpby
+from .batched import CsrBatch
 from .convert import convert, convert_inplace, from_coo, is_sorted, sort_by_row_and_column, to_coo
 from .containers import (COO_FORMAT, CSR_FORMAT, DIA_FORMAT, ELL_FORMAT, HDC_FORMAT, HYB_FORMAT,
                          INVALID_INDEX, NFORMATS, CooMatrix, CsrMatrix, DiaMatrix, DynamicMatrix,

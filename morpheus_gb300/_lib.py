@@ -43,6 +43,11 @@ class Ell(C.Structure):
                 ("width", i64), ("pitch", i64), ("column_indices", vp), ("values", vp)]
 
 
+class BatchItem(C.Structure):
+    _fields_ = [("nrows", i64), ("ncols", i64), ("nnz", i64), ("row_offsets", vp), ("column_indices", vp),
+                ("values", vp), ("x", vp), ("y", vp)]
+
+
 class Hyb(C.Structure):
     _fields_ = [("ell", Ell), ("coo", Coo)]
 
@@ -66,6 +71,14 @@ for _dt, _ct in (("f64", C.c_double), ("f32", C.c_float)):
     _SIGS[f"mgb_reduce_{_dt}"] = (C.c_int, [vp, i64, C.POINTER(_ct), vp])
     _SIGS[f"mgb_reduce_{_dt}_async"] = (C.c_int, [vp, i64, vp, vp])
     _SIGS[f"mgb_waxpby_{_dt}"] = (C.c_int, [i64, _ct, vp, _ct, vp, vp, vp])
+_SIGS["mgb_spmv_batched_csr_num_configs"] = (C.c_int, [])
+_SIGS["mgb_spmv_batched_csr_config_info"] = (C.c_int, [C.c_int, C.POINTER(i64), C.POINTER(C.c_int)])
+_SIGS["mgb_spmv_batched_csr_workspace_bytes"] = (C.c_int, [i64, C.POINTER(i64)])
+_SIGS["mgb_spmv_batched_csr_plan"] = (C.c_int, [vp, i64, C.c_int, vp, i64, vp])
+for _dt in ("f64", "f32"):
+    _SIGS[f"mgb_spmv_batched_csr_{_dt}"] = (C.c_int, [vp, i64, C.c_int, vp, C.c_int, vp])
+    _SIGS[f"mgb_spmv_batched_csr_autotune_{_dt}"] = (C.c_int, [vp, i64, vp, i64, C.c_int, C.POINTER(C.c_int),
+                                                               C.POINTER(C.c_float), vp])
 _SIGS["mgb_spmv_coo_f64_noalloc"] = (C.c_int, [C.POINTER(Coo), vp, vp, C.c_int, vp])
 _P = C.POINTER
 for _name, _s, _d in (("csr_to_coo", Csr, Coo), ("coo_to_csr", Coo, Csr), ("dia_to_coo", Dia, Coo),

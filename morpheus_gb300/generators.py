@@ -19,6 +19,8 @@ Workloads (sizes of the reference configurations):
 """
 from __future__ import annotations
 
+import math
+
 import numpy as np
 
 CSR = 1
@@ -287,3 +289,29 @@ def csr_to_hdc_host(A: dict, alignment: int = 32, ratio: float = 0.2) -> dict:
            "values": A["values"][~is_dia].copy()}
     return {"format": 5, "nrows": N, "ncols": M, "nnz": A["nnz"], "alignment": alignment,
             "dia": dia, "csr": csr}
+
+
+def batched_csr(count: int = 4096, nmin: int = 64, nmax: int = 8192, lam_lo: float = 3.0, lam_hi: float = 40.0,
+                seed: int = 0, dtype=np.float64) -> list[dict]:
+    """Independent square CSR matrices: N log-uniform in [nmin, nmax], row
+    lengths Poisson(lambda) with lambda ~ U[lam_lo, lam_hi] per matrix, distinct
+    uniform columns (sorted), N(0,1) values."""
+    rng = _rng(seed)
+    out = []
+    for _ in range(count):
+        N = int(round(math.exp(rng.uniform(math.log(nmin), math.log(nmax)))))
+        lam = rng.uniform(lam_lo, lam_hi)
+        lens = np.minimum(rng.poisson(lam, N), N).astype(np.int64)
+        rows = np.repeat(np.arange(N, dtype=np.int64), lens)
+        keys = rows * N + rng.integers(0, N, rows.size, dtype=np.int64)
+        keys.sort()
+        while True:
+            dup = np.flatnonzero(keys[1:] == keys[:-1]) + 1
+            if dup.size == 0:
+                break
+            keys[dup] = (keys[dup] // N) * N + rng.integers(0, N, dup.size, dtype=np.int64)
+            keys.sort()
+        r = keys // N
+        vals = _nonzero_normal(rng, keys.size, dtype)
+        out.append(csr_from_sorted_keys(N, N, r, keys - r * N, vals))
+    return out
