@@ -182,6 +182,39 @@ int mgb_reduce_f32_async(const float* in, int64_t size, float* d_result, void* s
 int mgb_waxpby_f64(int64_t n, double alpha, const double* x, double beta, const double* y, double* w, void* stream);
 int mgb_waxpby_f32(int64_t n, float alpha, const float* x, float beta, const float* y, float* w, void* stream);
 
+/* ---- analytics and format selection ---------------------------------------
+ * Morpheus analytics (core/src/Morpheus_MatrixAnalytics.hpp:85-261) from one
+ * pass over a CSR matrix, written to out14 (host):
+ *   [0] average_nnnz  [1] density  [2] max_nnnz  [3] min_nnnz
+ *   [4] std_nnnz (FP64; the reference truncates it to an integer)
+ *   [5] count_diagonals  [6] count_true_diagonals (>= floor(0.2 N) entries)
+ *   [7] entries on true diagonals  [8] bandwidth max|c - r|
+ *   [9] entries beyond the mean ELL width (size of a reference HYB's COO part)
+ *   [10..13] 1 if DIA / ELL / HYB / HDC pass the reference fill-tolerance test
+ * Synchronises the stream. */
+int mgb_analytics_csr(const mgb_csr* A, double* out14, void* stream);
+
+/* The format selector's 12 input features (host floats) and the feasibility
+ * mask of the six formats (host bytes, may be NULL); no reference counterpart
+ * (the reference's format choice is the --morpheus-format flag,
+ * impl/Morpheus_Core.cpp:101-125). */
+int mgb_features_csr(const mgb_csr* A, float* features12, uint8_t* feasible6, void* stream);
+
+/* Selector network 12 -> 64 -> 64 -> 6 (ReLU, softmax over feasible formats),
+ * FP32 device buffers.  params: mgb_mlp_num_params() floats; mu/sigma: the
+ * 12 standardisation constants; X: n x 12; feasible: n x 6 bytes (or NULL).
+ * forward writes log-probabilities (n x 6); grad writes the mean gradient of
+ * the cross-entropy loss over n samples and the mean loss (device scalar,
+ * may be NULL); adam applies one Adam step (step counts from 1). */
+int mgb_mlp_num_params(void);
+int mgb_mlp_forward_f32(const float* params, const float* mu, const float* sigma, const float* X,
+                        const uint8_t* feasible, int64_t n, float* logp, void* stream);
+int mgb_mlp_grad_f32(const float* params, const float* mu, const float* sigma, const float* X,
+                     const int32_t* labels, const uint8_t* feasible, int64_t n, float* grads, float* loss,
+                     void* stream);
+int mgb_mlp_adam_f32(float* params, const float* grads, float* m, float* v, int64_t nparams, float lr, float beta1,
+                     float beta2, float eps, int step, void* stream);
+
 /* ---- batched CSR SpMV ----------------------------------------------------
  * No counterpart in the reference, whose equivalent is one
  * Morpheus::multiply call per matrix (impl/Csr/Cuda/Morpheus_Multiply_Impl.hpp:94-157).

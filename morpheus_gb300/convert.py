@@ -120,8 +120,12 @@ def _deep_copy(A: _Matrix) -> _Matrix:
 
 
 def convert_inplace(dyn: DynamicMatrix, fmt, stream=None, hyb_width: int = 0) -> conversion_error_e:
-    """core/src/Morpheus_Convert.hpp:88-124"""
+    """core/src/Morpheus_Convert.hpp:88-124.  fmt = AUTO_FORMAT (-1) asks the
+    learned selector for the target format."""
     fmt = int(fmt)
+    if fmt == -1:
+        from .selector import select_format
+        fmt = select_format(dyn)
     if fmt < 0 or fmt >= NFORMATS:
         return conversion_error_e.PROXY_TO_DYNAMIC
     if dyn.active_index() == fmt:
