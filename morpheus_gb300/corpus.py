@@ -57,14 +57,17 @@ def generate(seed: int, device="cuda") -> tuple[CsrMatrix, dict]:
     N = int(round(math.exp(rng.uniform(math.log(1e4), math.log(4e6)))))
     dev = torch.device(device)
     desc = {"family": fam, "seed": seed}
+    cap = int(NNZ_CAP / 1.06)  # room for the off-pattern entries
     if fam == "banded":
         bw = int(rng.integers(1, 65))
-        bw = max(1, min(bw, (NNZ_CAP // N - 1) // 2))
+        bw = max(1, min(bw, (cap // N - 1) // 2))
+        N = min(N, cap // (2 * bw + 1))
         keys = _offsets_keys(N, range(-bw, bw + 1), dev)
         desc["bandwidth"] = bw
     elif fam == "block":
         b = int(rng.integers(4, 257))
-        b = max(1, min(b, NNZ_CAP // N))
+        b = max(1, min(b, cap // N))
+        N = min(N, cap // b)
         nb = (N + b - 1) // b
         i = torch.arange(b, device=dev, dtype=torch.int64)
         base = torch.arange(nb, device=dev, dtype=torch.int64) * b
@@ -75,22 +78,26 @@ def generate(seed: int, device="cuda") -> tuple[CsrMatrix, dict]:
         desc["block"] = b
     elif fam == "uniform":
         dens = math.exp(rng.uniform(math.log(1e-6), math.log(1e-3)))
-        nnz = int(min(NNZ_CAP, max(N, dens * N * N)))
+        nnz = int(min(cap, max(N, dens * N * N)))
         keys = torch.randint(0, N * N, (nnz,), generator=g, device=dev, dtype=torch.int64)
         desc["density"] = nnz / (N * N)
     elif fam == "lognormal":
         mu, sigma = rng.uniform(0.5, 3.0), rng.uniform(0.5, 1.5)
         lens = np.clip(np.rint(rng.lognormal(mu, sigma, N)), 1, 4096).astype(np.int64)
-        if lens.sum() > NNZ_CAP:
-            lens = np.maximum(1, (lens * (NNZ_CAP / lens.sum())).astype(np.int64))
+        N = min(N, cap)
+        lens = lens[:N]
+        if lens.sum() > cap:  # shrink the part above one entry per row
+            extra = lens - 1
+            lens = 1 + (extra * ((cap - N) / max(1, int(extra.sum())))).astype(np.int64)
         lt = torch.from_numpy(lens).to(dev)
         rows = torch.repeat_interleave(torch.arange(N, device=dev, dtype=torch.int64), lt)
         keys = rows * N + torch.randint(0, N, (rows.numel(),), generator=g, device=dev, dtype=torch.int64)
         desc.update(mu=mu, sigma=sigma)
     elif fam == "stencil2d":
         n = max(2, int(round(math.sqrt(N))))
-        N = n * n
         pts = 9 if rng.random() < 0.5 else 5
+        n = min(n, int(math.sqrt(cap / pts)))
+        N = n * n
         offs = [(a, b) for a in (-1, 0, 1) for b in (-1, 0, 1) if pts == 9 or abs(a) + abs(b) <= 1]
         r = torch.arange(N, device=dev, dtype=torch.int64)
         i, j = r // n, r % n
@@ -103,8 +110,8 @@ def generate(seed: int, device="cuda") -> tuple[CsrMatrix, dict]:
     else:
         n = max(2, int(round(N ** (1 / 3))))
         pts = 27 if rng.random() < 0.5 else 7
-        if n ** 3 * pts > NNZ_CAP:
-            n = int((NNZ_CAP / pts) ** (1 / 3))
+        if n ** 3 * pts > cap:
+            n = int((cap / pts) ** (1 / 3))
         N = n ** 3
         offs = [(a, b, c) for a in (-1, 0, 1) for b in (-1, 0, 1) for c in (-1, 0, 1)
                 if pts == 27 or abs(a) + abs(b) + abs(c) <= 1]

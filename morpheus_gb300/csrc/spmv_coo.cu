@@ -1,4 +1,4 @@
-// spmv_coo.cu -- COO SpMV for sm_103a (segmented reduction over row-sorted keys).
+// spmv_coo.cu -- COO SpMV for sm_103a (row-sorted keys).
 //
 // Replaces the reference's CUDA COO path (impl/Coo/Cuda/Morpheus_Multiply_Impl.hpp:50-176:
 // flat kernel impl/Coo/Kernels/Morpheus_Multiply_Impl.hpp:121-208, carry pass
@@ -8,164 +8,146 @@
 // Serial multiply (impl/Coo/Serial/Morpheus_Multiply_Impl.hpp:38-59):
 // y = 0 if init, then y[I[n]] += V[n] * x[J[n]].
 //
-// Design: one warp per chunk of COO_CH consecutive entries, staged through
-// shared memory with coalesced loads.  Row runs inside the chunk are found
-// with a ballot; each lane sums whole runs with one FMA per entry (runs longer
-// than COO_LONG are summed by the whole warp).  Interior runs are complete
-// rows and are stored directly.  The first and last run of every chunk may
-// continue in a neighbouring chunk, so they are written as carries and a
-// second, tiny kernel adds the carries of each row in chunk order:
-// deterministic, no atomics.  With init, rows without entries are zero-filled
-// by the chunk that sees the gap, so y is written exactly once and never read.
+// Design: fixed chunks of COO_CHUNK consecutive entries, one warp each, cut
+// into 32 contiguous lane ranges (the lane-segment scheme of spmv_csr.cu, so
+// every FP64 FMA is issued by all 32 lanes).  Row indices, columns and values
+// are staged through padded shared memory with coalesced loads; a lane
+// detects row ends by comparing consecutive row indices.  Rows that cross
+// lanes are combined by one segmented shuffle scan per chunk.  The first and
+// last row of a chunk may continue in a neighbouring chunk, so their sums are
+// written as carries and a small second kernel adds each row's carries in
+// chunk order; interior rows are stored directly: deterministic, no atomics,
+// no searches.  With init, rows without entries are zero-filled by the lane
+// that sees the gap, so y is written once per row.
 #include "mgb_internal.cuh"
 
 namespace mgb {
 namespace {
 
 constexpr int COO_WARPS = 8;
-constexpr int COO_CH = 256;
-constexpr int COO_LONG = 64;
+constexpr int COO_SEG = 8;                  // entries per lane per staging step
+constexpr int COO_PAD = COO_SEG + 1;        // padded lane stride in shared memory
+constexpr int64_t COO_CHUNK = 2048;         // entries per warp chunk
+constexpr int COO_KW = (int)(COO_CHUNK / 32);  // entries per lane
 
 template <typename T>
 __device__ __forceinline__ T gather_x(const T* __restrict__ x, int32_t c, int64_t ncols) {
   return ((uint64_t)(int64_t)c < (uint64_t)ncols) ? __ldg(x + c) : T(0);
 }
 
-// zero-fill rows (a, b) exclusive on both ends, cooperatively by the warp
-__device__ __forceinline__ void zero_gap_warp(int64_t a, int64_t b, int lane, double* y) {
-  for (int64_t r = a + 1 + lane; r < b; r += 32) y[r] = 0.0;
-}
-__device__ __forceinline__ void zero_gap_warp(int64_t a, int64_t b, int lane, float* y) {
-  for (int64_t r = a + 1 + lane; r < b; r += 32) y[r] = 0.0f;
-}
-
 template <typename T>
-__global__ void __launch_bounds__(COO_WARPS * 32, 4)
-spmv_coo_chunks(int64_t nrows, int64_t ncols, int64_t nnz,
-                const int32_t* __restrict__ ri, const int32_t* __restrict__ ci,
-                const T* __restrict__ va, const T* __restrict__ x,
-                T* __restrict__ y, int init, int32_t* __restrict__ carry_row,
-                T* __restrict__ carry_val) {
-  __shared__ int32_t s_row[COO_WARPS][COO_CH];
-  __shared__ int32_t s_col[COO_WARPS][COO_CH];
-  __shared__ T s_val[COO_WARPS][COO_CH];
-  __shared__ int16_t s_start[COO_WARPS][COO_CH + 1];
+__global__ void __launch_bounds__(COO_WARPS * 32, 3)
+spmv_coo_segments(int64_t nrows, int64_t ncols, int64_t nnz, const int32_t* __restrict__ ri,
+                  const int32_t* __restrict__ ci, const T* __restrict__ va, const T* __restrict__ x,
+                  T* __restrict__ y, int init, int32_t* __restrict__ carry_row, T* __restrict__ carry_val) {
+  __shared__ T s_val[COO_WARPS][32 * COO_PAD];
+  __shared__ int32_t s_col[COO_WARPS][32 * COO_PAD];
+  __shared__ int32_t s_row[COO_WARPS][32 * COO_PAD];
   const int lane = threadIdx.x & 31;
   const int w = threadIdx.x >> 5;
-  int32_t* sr = s_row[w];
-  int32_t* sc = s_col[w];
   T* sv = s_val[w];
-  int16_t* ss = s_start[w];
-  const unsigned lt_mask = (1u << lane) - 1u;
+  int32_t* sc = s_col[w];
+  int32_t* sr = s_row[w];
 
-  const int64_t nchunks = (nnz + COO_CH - 1) / COO_CH;
-  for (int64_t k = (int64_t)blockIdx.x * COO_WARPS + w; k < nchunks;
-       k += (int64_t)gridDim.x * COO_WARPS) {
-    const int64_t base = k * COO_CH;
-    const int cnt = (int)min((int64_t)COO_CH, nnz - base);
-    const int64_t prev_row = base > 0 ? (int64_t)ri[base - 1] : -1;
-#pragma unroll
-    for (int j = 0; j < COO_CH / 32; j++) {
-      const int idx = j * 32 + lane;
-      if (idx < cnt) {
-        sr[idx] = ldg_stream(ri + base + idx);
-        sc[idx] = ldg_stream(ci + base + idx);
-        sv[idx] = ldg_stream(va + base + idx);
-      }
-    }
-    __syncwarp();
-    // run starts
-    int nruns = 0;
-#pragma unroll
-    for (int g = 0; g < COO_CH / 32; g++) {
-      const int idx = g * 32 + lane;
-      const bool flag = idx < cnt && (idx == 0 || sr[idx] != sr[idx - 1]);
-      const unsigned bal = __ballot_sync(0xffffffffu, flag);
-      if (flag) ss[nruns + __popc(bal & lt_mask)] = (int16_t)idx;
-      nruns += __popc(bal);
-    }
-    if (lane == 0) ss[nruns] = (int16_t)cnt;
-    __syncwarp();
+  const int64_t nchunks = (nnz + COO_CHUNK - 1) / COO_CHUNK;
+  for (int64_t k = (int64_t)blockIdx.x * COO_WARPS + w; k < nchunks; k += (int64_t)gridDim.x * COO_WARPS) {
+    const int64_t base = k * COO_CHUNK;
+    const int64_t cend = min(base + COO_CHUNK, nnz);
+    const int64_t la = base + (int64_t)lane * COO_KW;
+    const int64_t lb = min(la + COO_KW, cend);
+    const bool active = la < lb;
+    const int64_t first_row = __ldg(ri + base);
+    const int64_t last_row = __ldg(ri + cend - 1);
+    // row of the entry before this lane's range, and of the entry after it
+    const int64_t prev = (active && la > 0) ? (int64_t)__ldg(ri + la - 1) : -1;
+    const int64_t next = (active && lb < cend) ? (int64_t)__ldg(ri + lb) : -2;
 
-    const bool last_chunk = (k == nchunks - 1);
-    // short runs: one lane per run
-    for (int j = lane; j < nruns; j += 32) {
-      const int a = ss[j], b = ss[j + 1];
-      const int64_t row = sr[a];
-      if (init) {
-        const int64_t before = (j == 0) ? prev_row : (int64_t)sr[ss[j - 1]];
-        if (row - before > 1 && row - before <= 33)
-          for (int64_t r = before + 1; r < row; r++)
-            if (r >= 0 && r < nrows) y[r] = T(0);
-        if (last_chunk && j == nruns - 1 && nrows - row > 1 && nrows - row <= 33)
-          for (int64_t r = row + 1; r < nrows; r++) y[r] = T(0);
-      }
-      if (b - a > COO_LONG) continue;
-      T s = T(0);
-      for (int e = a; e < b; e++) s = fmadd(sv[e], gather_x(x, sc[e], ncols), s);
-      if (j == 0) {
+    auto finalize = [&](int64_t row, T total) {
+      if (row == first_row) {
         carry_row[2 * k] = (int32_t)row;
-        carry_val[2 * k] = s;
-        if (nruns == 1) { carry_row[2 * k + 1] = (int32_t)row; carry_val[2 * k + 1] = T(0); }
-      } else if (j == nruns - 1) {
+        carry_val[2 * k] = total;
+        if (first_row == last_row) {
+          carry_row[2 * k + 1] = (int32_t)row;
+          carry_val[2 * k + 1] = T(0);
+        }
+      } else if (row == last_row) {
         carry_row[2 * k + 1] = (int32_t)row;
-        carry_val[2 * k + 1] = s;
+        carry_val[2 * k + 1] = total;
       } else if (row >= 0 && row < nrows) {
-        y[row] = init ? s : y[row] + s;
+        y[row] = total;
       }
-    }
-    // long gaps (init only): whole warp fills
-    if (init) {
-      for (int j0 = 0; j0 < nruns; j0 += 32) {
-        const int j = j0 + lane;
-        bool big = false;
-        int64_t lo_gap = 0, hi_gap = 0;
-        if (j < nruns) {
-          const int64_t row = sr[ss[j]];
-          const int64_t before = (j == 0) ? prev_row : (int64_t)sr[ss[j - 1]];
-          if (row - before > 33) { big = true; lo_gap = max(before, (int64_t)-1); hi_gap = min(row, nrows); }
-        }
-        unsigned m = __ballot_sync(0xffffffffu, big);
-        while (m) {
-          const int l = __ffs(m) - 1;
-          m &= m - 1;
-          zero_gap_warp(__shfl_sync(0xffffffffu, lo_gap, l), __shfl_sync(0xffffffffu, hi_gap, l), lane, y);
-        }
+    };
+    auto zero_gap = [&](int64_t from, int64_t to) {  // rows (from, to), init only
+      for (int64_t g = max(from + 1, (int64_t)0); g < min(to, nrows); g++) y[g] = T(0);
+    };
+
+    int64_t cur = -1;          // row being accumulated
+    bool cur_here = false;     // it started inside this lane's range
+    int64_t hrow = -1;
+    T hval = T(0), acc = T(0);
+
+    for (int st = 0; st < COO_KW; st += COO_SEG) {
+      __syncwarp();
+#pragma unroll
+      for (int q = 0; q < COO_SEG; q++) {
+        const int f = q * 32 + lane;
+        const int L = f / COO_SEG, j = f % COO_SEG;
+        const int64_t e = base + (int64_t)L * COO_KW + st + j;
+        const bool in = e < cend;
+        sr[L * COO_PAD + j] = in ? ldg_stream(ri + e) : -1;
+        sc[L * COO_PAD + j] = in ? ldg_stream(ci + e) : 0;
+        sv[L * COO_PAD + j] = in ? ldg_stream(va + e) : T(0);
       }
-      if (last_chunk) {
-        const int64_t row = sr[ss[nruns - 1]];
-        if (nrows - row > 33) zero_gap_warp(max(row, (int64_t)-1), nrows, lane, y);
+      __syncwarp();
+      T v[COO_SEG], xv[COO_SEG];
+      int32_t rw[COO_SEG];
+#pragma unroll
+      for (int kk = 0; kk < COO_SEG; kk++) {
+        const bool valid = la + st + kk < lb;
+        rw[kk] = sr[lane * COO_PAD + kk];
+        v[kk] = valid ? sv[lane * COO_PAD + kk] : T(0);
+        xv[kk] = valid ? gather_x(x, sc[lane * COO_PAD + kk], ncols) : T(0);
       }
-    }
-    // long runs: whole warp per run
-    for (int j0 = 0; j0 < nruns; j0 += 32) {
-      const int jj = j0 + lane;
-      const bool lng = jj < nruns && (ss[jj + 1] - ss[jj]) > COO_LONG;
-      unsigned m = __ballot_sync(0xffffffffu, lng);
-      while (m) {
-        const int l = __ffs(m) - 1;
-        m &= m - 1;
-        const int j = j0 + l;
-        const int a = ss[j], b = ss[j + 1];
-        T s = T(0);
-        for (int e = a + lane; e < b; e += 32) s = fmadd(sv[e], gather_x(x, sc[e], ncols), s);
-        s = warp_sum(s);
-        if (lane == 0) {
-          const int64_t row = sr[a];
-          if (j == 0) {
-            carry_row[2 * k] = (int32_t)row;
-            carry_val[2 * k] = s;
-            if (nruns == 1) { carry_row[2 * k + 1] = (int32_t)row; carry_val[2 * k + 1] = T(0); }
-          } else if (j == nruns - 1) {
-            carry_row[2 * k + 1] = (int32_t)row;
-            carry_val[2 * k + 1] = s;
-          } else if (row >= 0 && row < nrows) {
-            y[row] = init ? s : y[row] + s;
+#pragma unroll
+      for (int kk = 0; kk < COO_SEG; kk++) {
+        const int64_t e = la + st + kk;
+        if (e < lb && rw[kk] != cur) {  // a new row starts at e (or the lane's first row)
+          if (cur >= 0) {
+            if (cur_here) finalize(cur, acc); else { hrow = cur; hval = acc; }
           }
+          const int64_t before = (cur >= 0) ? cur : prev;
+          if (init && rw[kk] - before > 1) zero_gap(before, rw[kk]);
+          cur = rw[kk];
+          cur_here = (e > la) || (prev != cur);
+          const bool carried = (cur == first_row) || (cur == last_row);
+          acc = (init || carried || !cur_here || cur < 0 || cur >= nrows) ? T(0) : y[cur];
         }
+        acc = fmadd(v[kk], xv[kk], acc);
       }
     }
-    __syncwarp();
+    // the lane's last row: continues into the next lane, or ends here
+    bool has_tail = false;
+    if (active) {
+      if (next == cur) {
+        has_tail = true;
+      } else {
+        if (cur_here) finalize(cur, acc); else { hrow = cur; hval = acc; }
+      }
+    }
+    const int64_t key = has_tail ? cur : -1 - (int64_t)lane;
+    T cv = has_tail ? acc : T(0);
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const T u = __shfl_up_sync(0xffffffffu, cv, d);
+      const int64_t k2 = __shfl_up_sync(0xffffffffu, key, d);
+      if (lane >= d && k2 == key) cv += u;
+    }
+    const T vprev = __shfl_up_sync(0xffffffffu, cv, 1);
+    const int64_t kprev = __shfl_up_sync(0xffffffffu, key, 1);
+    if (hrow >= 0) finalize(hrow, (lane > 0 && kprev == hrow) ? hval + vprev : hval);
+    // rows after the last entry of the matrix (init): whole warp fills
+    if (init && k == nchunks - 1)
+      for (int64_t g = max(last_row + 1, (int64_t)0) + lane; g < nrows; g += 32) y[g] = T(0);
   }
 }
 
@@ -198,7 +180,7 @@ int launch_coo(const mgb_coo* A, const T* x, T* y, int init, cudaStream_t s) {
     return MGB_SUCCESS;
   }
   MGB_REQUIRE(A->row_indices && A->column_indices && A->values && x, MGB_ERR_BAD_ARGUMENT);
-  const int64_t nchunks = (A->nnz + COO_CH - 1) / COO_CH;
+  const int64_t nchunks = (A->nnz + COO_CHUNK - 1) / COO_CHUNK;
   const int64_t ncarry = 2 * nchunks;
   void* scratch = nullptr;
   const size_t rows_bytes = ((sizeof(int32_t) * ncarry + 255) / 256) * 256;
@@ -206,7 +188,7 @@ int launch_coo(const mgb_coo* A, const T* x, T* y, int init, cudaStream_t s) {
   int32_t* cr = static_cast<int32_t*>(scratch);
   T* cv = reinterpret_cast<T*>(static_cast<char*>(scratch) + rows_bytes);
   const int64_t blocks = (nchunks + COO_WARPS - 1) / COO_WARPS;
-  spmv_coo_chunks<T><<<(unsigned)blocks, COO_WARPS * 32, 0, s>>>(
+  spmv_coo_segments<T><<<(unsigned)blocks, COO_WARPS * 32, 0, s>>>(
       A->nrows, A->ncols, A->nnz, A->row_indices, A->column_indices,
       static_cast<const T*>(A->values), x, y, init, cr, cv);
   cudaError_t e = cudaGetLastError();
@@ -251,8 +233,8 @@ int mgb_spmv_coo_f32(const mgb_coo* A, const float* x, float* y, int init, void*
 // Limits and rules:
 //  * The array is COO_NOALLOC_BYTES (4 MiB) of device memory that every GPU
 //    which loads this library holds until the process exits.  It holds two
-//    carries (int32 row + double value) per 256-entry chunk, so A->nnz may be
-//    at most 44,736,512; larger matrices get MGB_ERR_INVALID_INPUT before any
+//    carries (int32 row + double value) per 2048-entry chunk, so A->nnz may be
+//    at most 357,892,096; larger matrices get MGB_ERR_INVALID_INPUT before any
 //    work is queued.
 //  * The first call on a device looks up the array's device address with
 //    cudaGetSymbolAddress (once per device, with that device current) and
@@ -298,7 +280,7 @@ int noalloc_scratch(void** out) {
 int launch_coo_noalloc_f64(const mgb_coo* A, const double* x, double* y, int init, cudaStream_t s) {
   MGB_REQUIRE(A != nullptr, MGB_ERR_BAD_ARGUMENT);
   MGB_REQUIRE(!bad_sizes(A->nrows, A->ncols, A->nnz), MGB_ERR_BAD_ARGUMENT);
-  const int64_t nchunks = (A->nnz + COO_CH - 1) / COO_CH;
+  const int64_t nchunks = (A->nnz + COO_CHUNK - 1) / COO_CHUNK;
   const int64_t ncarry = 2 * nchunks;
   const size_t rows_bytes = ((sizeof(int32_t) * (size_t)ncarry + 255) / 256) * 256;
   MGB_REQUIRE(rows_bytes + sizeof(double) * (size_t)ncarry <= COO_NOALLOC_BYTES, MGB_ERR_INVALID_INPUT);
@@ -316,7 +298,7 @@ int launch_coo_noalloc_f64(const mgb_coo* A, const double* x, double* y, int ini
   int32_t* cr = static_cast<int32_t*>(scratch);
   double* cv = reinterpret_cast<double*>(static_cast<char*>(scratch) + rows_bytes);
   const int64_t blocks = (nchunks + COO_WARPS - 1) / COO_WARPS;
-  spmv_coo_chunks<double><<<(unsigned)blocks, COO_WARPS * 32, 0, s>>>(
+  spmv_coo_segments<double><<<(unsigned)blocks, COO_WARPS * 32, 0, s>>>(
       A->nrows, A->ncols, A->nnz, A->row_indices, A->column_indices,
       static_cast<const double*>(A->values), x, y, init, cr, cv);
   MGB_LAUNCH_CHECK();

@@ -25,7 +25,7 @@ from morpheus_gb300 import generators as gen
 
 pytestmark = pytest.mark.gpu
 
-MAX_NNZ = 44_736_512  # the documented capacity of the fixed scratch array
+MAX_NNZ = 357_892_096  # the documented capacity of the fixed scratch array
 
 
 def _coo_device(hm):
