@@ -121,6 +121,19 @@ const char* mgb_last_cuda_error_string(void);
 int mgb_spmv_csr_f64(const mgb_csr* A, const double* x, double* y, int init, void* stream);
 int mgb_spmv_csr_f32(const mgb_csr* A, const float* x, float* y, int init, void* stream);
 
+/* CSR kernel choice.  The reference runs its thread-per-row kernel only when
+ * the user sets MATOPT_SHORT_ROWS (impl/Csr/Cuda/Morpheus_Multiply_Impl.hpp:59-92);
+ * here mgb_csr_choose_kernel measures the row lengths (one pass, synchronises)
+ * and returns MGB_CSR_ROWS for short rows of nearly equal length (stencils,
+ * banded and mesh matrices: the row-tile kernel, coalesced x reads) or
+ * MGB_CSR_SEGMENTS otherwise (the lane-segment kernel that mgb_spmv_csr_*
+ * always uses).  Callers cache the choice per matrix. */
+#define MGB_CSR_SEGMENTS 1
+#define MGB_CSR_ROWS 2
+int mgb_csr_choose_kernel(const mgb_csr* A, int* variant, void* stream);
+int mgb_spmv_csr_variant_f64(const mgb_csr* A, const double* x, double* y, int init, int variant, void* stream);
+int mgb_spmv_csr_variant_f32(const mgb_csr* A, const float* x, float* y, int init, int variant, void* stream);
+
 /* replaces impl/Coo/Cuda/Morpheus_Multiply_Impl.hpp:50-176.  Like the
  * reference's CUDA path, A must be sorted by row (columns in any order). */
 int mgb_spmv_coo_f64(const mgb_coo* A, const double* x, double* y, int init, void* stream);
@@ -131,7 +144,7 @@ int mgb_spmv_coo_f32(const mgb_coo* A, const float* x, float* y, int init, void*
  * (code inside an allocation-free graph-capture region, hosts that reserve all
  * device memory up front, plugins whose host owns the allocator): the carry
  * buffer is a fixed 4 MiB file-scope device array instead of cudaMallocAsync,
- * and no allocating call is made.  Limits: A->nnz <= 44,736,512, otherwise
+ * and no allocating call is made.  Limits: A->nnz <= 357,892,096, otherwise
  * MGB_ERR_INVALID_INPUT before any work is queued; every GPU that loads the
  * library holds the 4 MiB until exit; the first call on a device looks up the
  * array's address (make it before any stream capture); all calls share the

@@ -71,6 +71,9 @@ for _dt, _ct in (("f64", C.c_double), ("f32", C.c_float)):
     _SIGS[f"mgb_reduce_{_dt}"] = (C.c_int, [vp, i64, C.POINTER(_ct), vp])
     _SIGS[f"mgb_reduce_{_dt}_async"] = (C.c_int, [vp, i64, vp, vp])
     _SIGS[f"mgb_waxpby_{_dt}"] = (C.c_int, [i64, _ct, vp, _ct, vp, vp, vp])
+_SIGS["mgb_csr_choose_kernel"] = (C.c_int, [C.POINTER(Csr), C.POINTER(C.c_int), vp])
+for _dt in ("f64", "f32"):
+    _SIGS[f"mgb_spmv_csr_variant_{_dt}"] = (C.c_int, [C.POINTER(Csr), vp, vp, C.c_int, C.c_int, vp])
 _SIGS["mgb_analytics_csr"] = (C.c_int, [C.POINTER(Csr), C.POINTER(C.c_double), vp])
 _SIGS["mgb_features_csr"] = (C.c_int, [C.POINTER(Csr), C.POINTER(C.c_float), C.POINTER(C.c_uint8), vp])
 _SIGS["mgb_mlp_num_params"] = (C.c_int, [])

@@ -44,6 +44,8 @@ class conversion_error_e(enum.IntEnum):
 
 COO_FORMAT, CSR_FORMAT, DIA_FORMAT, ELL_FORMAT, HYB_FORMAT, HDC_FORMAT, NFORMATS = range(7)
 INVALID_INDEX = -1
+# CSR SpMV kernels (MGB_CSR_SEGMENTS / MGB_CSR_ROWS of include/mgb.h)
+CSR_SEGMENTS, CSR_ROWS = 1, 2
 
 
 def get_pad_size(length: int, alignment: int) -> int:
@@ -150,6 +152,7 @@ class CsrMatrix(_Matrix):
         self._v = _as(values, dtype, self.device) if values is not None else _val(nnz, dtype, self.device)
         if self._ro.numel() != self._nrows + 1 or self._ci.numel() != self._nnz or self._v.numel() != self._nnz:
             raise InvalidInputException("CSR arrays have the wrong sizes")
+        self._variant = None
 
     def row_offsets(self): return self._ro
     def column_indices(self): return self._ci
@@ -157,6 +160,21 @@ class CsrMatrix(_Matrix):
     crow_offsets = row_offsets
     ccolumn_indices = column_indices
     cvalues = values
+
+    def kernel_variant(self) -> int:
+        """SpMV kernel for this matrix (CSR_ROWS for short rows of nearly
+        equal length, else CSR_SEGMENTS), measured once on the device and
+        cached.  Values may change in place; after writing new row offsets in
+        place, call forget_kernel_variant()."""
+        if self._variant is None:
+            out = C.c_int()
+            d = self._desc()
+            _lib.call("mgb_csr_choose_kernel", C.byref(d), C.byref(out), None)
+            self._variant = out.value
+        return self._variant
+
+    def forget_kernel_variant(self) -> None:
+        self._variant = None
 
     def resize(self, nrows, ncols, nnz):
         self.__init__(nrows, ncols, nnz, dtype=self.dtype, device=self.device)

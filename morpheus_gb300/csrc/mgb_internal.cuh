@@ -58,6 +58,8 @@ template <typename T>
 int launch_ell(const mgb_ell* A, const T* x, T* y, int init, cudaStream_t s);
 template <typename T>
 int launch_coo(const mgb_coo* A, const T* x, T* y, int init, cudaStream_t s);
+template <typename T>
+int launch_csr_rows(const mgb_csr* A, const T* x, T* y, int init, cudaStream_t s);
 
 // Validation helpers for descriptors.
 inline bool bad_sizes(int64_t a, int64_t b, int64_t c) { return a < 0 || b < 0 || c < 0; }

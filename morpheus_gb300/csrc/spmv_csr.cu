@@ -53,13 +53,15 @@ spmv_csr_segments(int64_t nrows, int64_t ncols, int64_t nnz, int64_t nchunks,
 }
 
 template <typename T>
-int launch_csr(const mgb_csr* A, const T* x, T* y, int init, void* stream) {
+int launch_csr(const mgb_csr* A, const T* x, T* y, int init, void* stream, int variant = MGB_CSR_SEGMENTS) {
   MGB_REQUIRE(A != nullptr, MGB_ERR_BAD_ARGUMENT);
   MGB_REQUIRE(!bad_sizes(A->nrows, A->ncols, A->nnz), MGB_ERR_BAD_ARGUMENT);
   MGB_REQUIRE(A->nnz < ((int64_t)1 << 31) - 4096, MGB_ERR_INVALID_INPUT);
+  MGB_REQUIRE(variant == MGB_CSR_SEGMENTS || variant == MGB_CSR_ROWS, MGB_ERR_BAD_ARGUMENT);
   if (A->nrows == 0) return MGB_SUCCESS;
   MGB_REQUIRE(A->row_offsets != nullptr && y != nullptr, MGB_ERR_BAD_ARGUMENT);
   MGB_REQUIRE(A->nnz == 0 || (A->column_indices && A->values && x), MGB_ERR_BAD_ARGUMENT);
+  if (variant == MGB_CSR_ROWS) return launch_csr_rows<T>(A, x, y, init, as_stream(stream));
   // one extra chunk so rows whose first entry is at nnz (trailing empty rows)
   // always belong to some chunk
   const int64_t nchunks = A->nnz / csr::CSR_CHUNK + 1;
@@ -83,6 +85,14 @@ int mgb_spmv_csr_f64(const mgb_csr* A, const double* x, double* y, int init, voi
 
 int mgb_spmv_csr_f32(const mgb_csr* A, const float* x, float* y, int init, void* stream) {
   return mgb::launch_csr<float>(A, x, y, init, stream);
+}
+
+int mgb_spmv_csr_variant_f64(const mgb_csr* A, const double* x, double* y, int init, int variant, void* stream) {
+  return mgb::launch_csr<double>(A, x, y, init, stream, variant);
+}
+
+int mgb_spmv_csr_variant_f32(const mgb_csr* A, const float* x, float* y, int init, int variant, void* stream) {
+  return mgb::launch_csr<float>(A, x, y, init, stream, variant);
 }
 
 }  // extern "C"

@@ -19,8 +19,10 @@ pytestmark = pytest.mark.gpu
 TOL = {np.float64: 1e-12, np.float32: 1e-5}
 
 
-def gpu_multiply(hm, x, y0, init):
+def gpu_multiply(hm, x, y0, init, csr_variant=None):
     A = mgb.matrix_from_host(hm, device="cuda")
+    if csr_variant is not None:
+        A._variant = csr_variant  # force one of the two CSR kernels
     xt = torch.from_numpy(x).cuda()
     yt = torch.from_numpy(y0.copy()).cuda()
     mgb.multiply(A, xt, yt, init=init)
@@ -28,13 +30,13 @@ def gpu_multiply(hm, x, y0, init):
     return yt.cpu().numpy()
 
 
-def check(hm, dtype, init=True, seed=0):
+def check(hm, dtype, init=True, seed=0, csr_variant=None):
     n, m = hm["nrows"], hm["ncols"]
     x = gen.x_vector(m, seed=seed, dtype=dtype)
     y0 = gen.x_vector(n, seed=seed + 1, dtype=dtype)
     om = O.OracleMatrix.from_host(hm)
     ref = om.multiply(x, y0.copy(), init=init)
-    y = gpu_multiply(hm, x, y0, init)
+    y = gpu_multiply(hm, x, y0, init, csr_variant)
     err = rel_err(y, ref)
     if dtype == np.float64:
         assert err <= TOL[dtype], f"rel err {err:.3e}"
@@ -163,6 +165,47 @@ def test_edge_cases(cuda, case, dtype):
             if hm["nnz"] == 0 and name in ("DIA", "HDC") and hm["nrows"] == 0:
                 continue
             check(hm, dtype, init)
+
+
+def _csr_case(case, dtype):
+    if case == "stencil27":
+        return gen.stencil_27pt(20, seed=21, dtype=dtype)
+    if case == "laplacian":
+        return gen.laplacian_2d(90, dtype=dtype)
+    if case == "banded":
+        return gen.banded(3001, diag_freq=500, seed=22, dtype=dtype)
+    if case == "power_law":
+        return gen.power_law(20000, seed=23, dtype=dtype)
+    if case == "empty_rows":
+        return gen.random_csr(4000, 4000, 0.003, seed=24, dtype=dtype, empty_row_frac=0.4)
+    if case == "long_rows":  # rows longer than one staged tile piece
+        lens = np.full(100, 3)
+        lens[[0, 31, 32, 77]] = [5000, 1200, 40000, 897]
+        return gen.random_lengths_csr(100, 50000, lens, seed=25, dtype=dtype)
+    if case == "ragged_tail":  # nrows not a multiple of 32
+        return gen.random_lengths_csr(1000 * 32 + 7, 5000, np.full(32007, 9), seed=26, dtype=dtype)
+    raise ValueError(case)
+
+
+@pytest.mark.parametrize("variant", [mgb.CSR_SEGMENTS, mgb.CSR_ROWS])
+@pytest.mark.parametrize("case", ["stencil27", "laplacian", "banded", "power_law", "empty_rows",
+                                  "long_rows", "ragged_tail"])
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_csr_kernel_variants(cuda, variant, case, dtype):
+    """Both CSR kernels give the Serial result on every structure, whichever
+    the per-matrix choice would pick."""
+    A = _csr_case(case, dtype)
+    for init in (True, False):
+        check(A, dtype, init, csr_variant=variant)
+
+
+@pytest.mark.parametrize("case,expect", [("stencil27", "rows"), ("laplacian", "rows"), ("banded", "rows"),
+                                         ("power_law", "segments"), ("long_rows", "segments"),
+                                         ("empty_rows", "segments")])
+def test_csr_kernel_choice(cuda, case, expect):
+    A = mgb.matrix_from_host(_csr_case(case, np.float64), device="cuda")
+    want = mgb.CSR_ROWS if expect == "rows" else mgb.CSR_SEGMENTS
+    assert A.kernel_variant() == want
 
 
 def test_deterministic(cuda):
