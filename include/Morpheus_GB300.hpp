@@ -230,7 +230,13 @@ class CsrMatrix {  // core/src/Morpheus_CsrMatrix.hpp:533-537
   void resize(int64_t r, int64_t c, int64_t n) {
     nrows_ = r; ncols_ = c; nnz_ = n;
     ro_.resize(r + 1); ci_.resize(n); v_.resize(n);
+    variant_ = 0;
   }
+  // SpMV kernel of this matrix (MGB_CSR_ROWS or MGB_CSR_SEGMENTS), measured
+  // on the device at the first multiply and cached.  Call
+  // forget_kernel_variant() after writing new row offsets.
+  int kernel_variant() const;
+  void forget_kernel_variant() { variant_ = 0; }
   int64_t nrows() const { return nrows_; }
   int64_t ncols() const { return ncols_; }
   int64_t nnnz() const { return nnz_; }
@@ -251,7 +257,19 @@ class CsrMatrix {  // core/src/Morpheus_CsrMatrix.hpp:533-537
   int64_t nrows_ = 0, ncols_ = 0, nnz_ = 0;
   DeviceArray<int32_t> ro_, ci_;
   DeviceArray<ValueType> v_;
+  mutable int variant_ = 0;
 };
+
+template <class ValueType>
+int CsrMatrix<ValueType>::kernel_variant() const {
+  if (variant_ == 0) {
+    mgb_csr d = desc();
+    int v = MGB_CSR_SEGMENTS;
+    Impl::check(mgb_csr_choose_kernel(&d, &v, nullptr), "CsrMatrix::kernel_variant");
+    variant_ = v;
+  }
+  return variant_;
+}
 
 template <class ValueType>
 class DiaMatrix {  // core/src/Morpheus_DiaMatrix.hpp:192-201, values (pad(N,32) x ndiags) column-major
@@ -392,9 +410,13 @@ class DynamicMatrix {
   using variant_type = std::variant<CooMatrix<ValueType>, CsrMatrix<ValueType>, DiaMatrix<ValueType>,
                                     EllMatrix<ValueType>, HybMatrix<ValueType>, HdcMatrix<ValueType>>;
   DynamicMatrix() = default;
-  template <class M>
+  DynamicMatrix(const DynamicMatrix&) = default;
+  DynamicMatrix(DynamicMatrix&&) noexcept = default;
+  DynamicMatrix& operator=(const DynamicMatrix&) = default;
+  DynamicMatrix& operator=(DynamicMatrix&&) noexcept = default;
+  template <class M, class = std::enable_if_t<!std::is_same_v<std::decay_t<M>, DynamicMatrix>>>
   DynamicMatrix(M m) : v_(std::move(m)) {}
-  template <class M>
+  template <class M, class = std::enable_if_t<!std::is_same_v<std::decay_t<M>, DynamicMatrix>>>
   DynamicMatrix& operator=(M m) {
     v_ = std::move(m);
     return *this;
@@ -402,9 +424,10 @@ class DynamicMatrix {
   int active_index() const { return (int)v_.index(); }
   formats_e active_enum() const { return (formats_e)v_.index(); }
   // Switches to an EMPTY container of the new format (no data is converted);
-  // an index past the last format leaves the matrix unchanged
-  // (core/src/Morpheus_DynamicMatrix.hpp:409-442).
+  // the active format, or an index past the last format, leaves the matrix
+  // unchanged (core/src/Morpheus_DynamicMatrix.hpp:409-442).
   void activate(int idx) {
+    if (idx == active_index()) return;
     switch (idx) {
       case COO_FORMAT: v_ = CooMatrix<ValueType>(); break;
       case CSR_FORMAT: v_ = CsrMatrix<ValueType>(); break;
@@ -435,7 +458,9 @@ constexpr void require_gb300() {
 }
 template <class T> struct Suffix;
 template <> struct Suffix<double> {
-  static int csr(const mgb_csr* a, const double* x, double* y, int i, void* s) { return mgb_spmv_csr_f64(a, x, y, i, s); }
+  static int csr(const mgb_csr* a, const double* x, double* y, int i, int v, void* s) {
+    return mgb_spmv_csr_variant_f64(a, x, y, i, v, s);
+  }
   static int coo(const mgb_coo* a, const double* x, double* y, int i, void* s) { return mgb_spmv_coo_f64(a, x, y, i, s); }
   static int dia(const mgb_dia* a, const double* x, double* y, int i, void* s) { return mgb_spmv_dia_f64(a, x, y, i, s); }
   static int ell(const mgb_ell* a, const double* x, double* y, int i, void* s) { return mgb_spmv_ell_f64(a, x, y, i, s); }
@@ -448,7 +473,9 @@ template <> struct Suffix<double> {
   }
 };
 template <> struct Suffix<float> {
-  static int csr(const mgb_csr* a, const float* x, float* y, int i, void* s) { return mgb_spmv_csr_f32(a, x, y, i, s); }
+  static int csr(const mgb_csr* a, const float* x, float* y, int i, int v, void* s) {
+    return mgb_spmv_csr_variant_f32(a, x, y, i, v, s);
+  }
   static int coo(const mgb_coo* a, const float* x, float* y, int i, void* s) { return mgb_spmv_coo_f32(a, x, y, i, s); }
   static int dia(const mgb_dia* a, const float* x, float* y, int i, void* s) { return mgb_spmv_dia_f32(a, x, y, i, s); }
   static int ell(const mgb_ell* a, const float* x, float* y, int i, void* s) { return mgb_spmv_ell_f32(a, x, y, i, s); }
@@ -464,7 +491,7 @@ template <> struct Suffix<float> {
 template <class T>
 void spmv(const CsrMatrix<T>& A, const T* x, T* y, bool init) {
   auto d = A.desc();
-  check(Suffix<T>::csr(&d, x, y, init, nullptr), "multiply<GB300>(CsrMatrix)");
+  check(Suffix<T>::csr(&d, x, y, init, A.kernel_variant(), nullptr), "multiply<GB300>(CsrMatrix)");
 }
 template <class T>
 void spmv(const CooMatrix<T>& A, const T* x, T* y, bool init) {
@@ -538,6 +565,188 @@ inline void waxpby(size_t n, typename Vector1::value_type alpha, const Vector1& 
   Impl::check(Impl::Suffix<typename Vector1::value_type>::waxpby((int64_t)n, alpha, x.data(), beta, y.data(),
                                                                  w.data()),
               "waxpby<GB300>");
+}
+
+// -------------------------------------------------------------- convert ---
+// Every pair goes through COO on the device (impl/Morpheus_Convert_Impl.hpp:82-104);
+// the structures are bit-identical to the reference's Serial convert.
+namespace Impl {
+template <class T> struct Conv;
+#define MGB_CONV_ENTRIES(SFX)                                                                                      \
+  static int csr_to_coo(const mgb_csr* s, mgb_coo* d) { return mgb_convert_csr_to_coo_##SFX(s, d, nullptr); }    \
+  static int coo_to_csr(const mgb_coo* s, mgb_csr* d) { return mgb_convert_coo_to_csr_##SFX(s, d, nullptr); }    \
+  static int dia_to_coo(const mgb_dia* s, mgb_coo* d) { return mgb_convert_dia_to_coo_##SFX(s, d, nullptr); }    \
+  static int coo_to_dia(const mgb_coo* s, mgb_dia* d) { return mgb_convert_coo_to_dia_##SFX(s, d, nullptr); }    \
+  static int ell_to_coo(const mgb_ell* s, mgb_coo* d) { return mgb_convert_ell_to_coo_##SFX(s, d, nullptr); }    \
+  static int coo_to_ell(const mgb_coo* s, mgb_ell* d) { return mgb_convert_coo_to_ell_##SFX(s, d, nullptr); }    \
+  static int hyb_to_coo(const mgb_hyb* s, mgb_coo* d) { return mgb_convert_hyb_to_coo_##SFX(s, d, nullptr); }    \
+  static int coo_to_hyb(const mgb_coo* s, mgb_hyb* d) { return mgb_convert_coo_to_hyb_##SFX(s, d, nullptr); }    \
+  static int hdc_to_coo(const mgb_hdc* s, mgb_coo* d) { return mgb_convert_hdc_to_coo_##SFX(s, d, nullptr); }    \
+  static int coo_to_hdc(const mgb_coo* s, mgb_hdc* d) { return mgb_convert_coo_to_hdc_##SFX(s, d, nullptr); }    \
+  static int sort(mgb_coo* a) { return mgb_coo_sort_by_row_and_column_##SFX(a, nullptr); }
+template <> struct Conv<double> { MGB_CONV_ENTRIES(f64) };
+template <> struct Conv<float> { MGB_CONV_ENTRIES(f32) };
+#undef MGB_CONV_ENTRIES
+
+// X -> COO
+template <class T>
+CooMatrix<T> to_coo(const CooMatrix<T>& A) { return A; }
+template <class T>
+CooMatrix<T> to_coo(const CsrMatrix<T>& A) {
+  CooMatrix<T> out(A.nrows(), A.ncols(), A.nnnz());
+  mgb_csr s = A.desc();
+  mgb_coo d = out.desc();
+  check(Conv<T>::csr_to_coo(&s, &d), "convert<GB300>(CsrMatrix -> CooMatrix)");
+  return out;
+}
+template <class T>
+CooMatrix<T> to_coo(const DiaMatrix<T>& A) {
+  CooMatrix<T> out(A.nrows(), A.ncols(), A.nnnz());
+  mgb_dia s = A.desc();
+  mgb_coo d = out.desc();
+  check(Conv<T>::dia_to_coo(&s, &d), "convert<GB300>(DiaMatrix -> CooMatrix)");
+  return out;
+}
+template <class T>
+CooMatrix<T> to_coo(const EllMatrix<T>& A) {
+  CooMatrix<T> out(A.nrows(), A.ncols(), A.nnnz());
+  mgb_ell s = A.desc();
+  mgb_coo d = out.desc();
+  check(Conv<T>::ell_to_coo(&s, &d), "convert<GB300>(EllMatrix -> CooMatrix)");
+  return out;
+}
+template <class T>
+CooMatrix<T> to_coo(const HybMatrix<T>& A) {
+  CooMatrix<T> out(A.nrows(), A.ncols(), A.nnnz());
+  mgb_hyb s = A.desc();
+  mgb_coo d = out.desc();
+  check(Conv<T>::hyb_to_coo(&s, &d), "convert<GB300>(HybMatrix -> CooMatrix)");
+  return out;
+}
+template <class T>
+CooMatrix<T> to_coo(const HdcMatrix<T>& A) {
+  CooMatrix<T> out(A.nrows(), A.ncols(), A.nnnz());
+  mgb_hdc s = A.desc();
+  mgb_coo d = out.desc();
+  check(Conv<T>::hdc_to_coo(&s, &d), "convert<GB300>(HdcMatrix -> CooMatrix)");
+  return out;
+}
+template <class T>
+CooMatrix<T> to_coo(const DynamicMatrix<T>& A) {
+  return std::visit([](const auto& m) { return to_coo(m); }, A.const_formats());
+}
+
+// COO -> Y (sizes from the *_plan calls, which also apply the fill tolerance)
+template <class T>
+void from_coo(const CooMatrix<T>& A, CooMatrix<T>& out) { out = A; }
+template <class T>
+void from_coo(const CooMatrix<T>& A, CsrMatrix<T>& out) {
+  mgb_coo s = A.desc();
+  CsrMatrix<T> r(A.nrows(), A.ncols(), A.nnnz());
+  mgb_csr d = r.desc();
+  check(Conv<T>::coo_to_csr(&s, &d), "convert<GB300>(CooMatrix -> CsrMatrix)");
+  out = std::move(r);
+}
+template <class T>
+void from_coo(const CooMatrix<T>& A, DiaMatrix<T>& out) {
+  mgb_coo s = A.desc();
+  int64_t nd = 0;
+  check(mgb_convert_coo_to_dia_plan(&s, &nd, nullptr), "convert<GB300>(CooMatrix -> DiaMatrix)");
+  DiaMatrix<T> r(A.nrows(), A.ncols(), A.nnnz(), nd);
+  mgb_dia d = r.desc();
+  check(Conv<T>::coo_to_dia(&s, &d), "convert<GB300>(CooMatrix -> DiaMatrix)");
+  out = std::move(r);
+}
+template <class T>
+void from_coo(const CooMatrix<T>& A, EllMatrix<T>& out) {
+  mgb_coo s = A.desc();
+  int64_t w = 0;
+  check(mgb_convert_coo_to_ell_plan(&s, &w, nullptr), "convert<GB300>(CooMatrix -> EllMatrix)");
+  EllMatrix<T> r(A.nrows(), A.ncols(), A.nnnz(), w);
+  mgb_ell d = r.desc();
+  check(Conv<T>::coo_to_ell(&s, &d), "convert<GB300>(CooMatrix -> EllMatrix)");
+  out = std::move(r);
+}
+template <class T>
+void from_coo(const CooMatrix<T>& A, HybMatrix<T>& out) {
+  mgb_coo s = A.desc();
+  int64_t w = 0, ell_nnz = 0, coo_nnz = 0;
+  check(mgb_convert_coo_to_hyb_plan(&s, 0, &w, &ell_nnz, &coo_nnz, nullptr), "convert<GB300>(CooMatrix -> HybMatrix)");
+  HybMatrix<T> r(EllMatrix<T>(A.nrows(), A.ncols(), ell_nnz, w), CooMatrix<T>(A.nrows(), A.ncols(), coo_nnz));
+  mgb_hyb d = r.desc();
+  check(Conv<T>::coo_to_hyb(&s, &d), "convert<GB300>(CooMatrix -> HybMatrix)");
+  out = std::move(r);
+}
+template <class T>
+void from_coo(const CooMatrix<T>& A, HdcMatrix<T>& out) {
+  mgb_coo s = A.desc();
+  int64_t nd = 0, dia_nnz = 0, csr_nnz = 0;
+  check(mgb_convert_coo_to_hdc_plan(&s, &nd, &dia_nnz, &csr_nnz, nullptr), "convert<GB300>(CooMatrix -> HdcMatrix)");
+  HdcMatrix<T> r(DiaMatrix<T>(A.nrows(), A.ncols(), dia_nnz, nd), CsrMatrix<T>(A.nrows(), A.ncols(), csr_nnz));
+  mgb_hdc d = r.desc();
+  check(Conv<T>::coo_to_hdc(&s, &d), "convert<GB300>(CooMatrix -> HdcMatrix)");
+  out = std::move(r);
+}
+template <class T>
+void from_coo(const CooMatrix<T>& A, DynamicMatrix<T>& out) {  // keeps the active format of out
+  std::visit([&](auto& m) { from_coo(A, m); }, out.formats());
+}
+}  // namespace Impl
+
+// core/src/Morpheus_Convert.hpp:53-57: src and dst of any (possibly the same)
+// formats, including DynamicMatrix on either side.
+template <class ExecSpace, class SourceType, class DestinationType>
+void convert(const SourceType& src, DestinationType& dst) {
+  Impl::require_gb300<ExecSpace>();
+  Impl::from_coo(Impl::to_coo(src), dst);
+}
+
+// core/src/Morpheus_Convert.hpp:88-124: in-place switch of a DynamicMatrix
+// with the reference's error codes (the source is left unchanged on error).
+template <class ExecSpace, class ValueType>
+conversion_error_e convert(DynamicMatrix<ValueType>& A, const formats_e index) {
+  Impl::require_gb300<ExecSpace>();
+  const int idx = (int)index;
+  if (idx < 0 || idx >= (int)NFORMATS) return PROXY_TO_DYNAMIC;
+  if (A.active_index() == idx) return CONV_SUCCESS;
+  CooMatrix<ValueType> temp;
+  try {
+    temp = Impl::to_coo(A);
+  } catch (const Exception&) {
+    return DYNAMIC_TO_PROXY;
+  }
+  DynamicMatrix<ValueType> out;
+  out.activate(idx);
+  try {
+    Impl::from_coo(temp, out);
+  } catch (const Exception&) {
+    return PROXY_TO_DYNAMIC;
+  }
+  A = std::move(out);
+  return CONV_SUCCESS;
+}
+
+// core/src/Morpheus_Convert.hpp:126-141
+template <class ExecSpace, class ValueType>
+conversion_error_e convert(DynamicMatrix<ValueType>& A, const int idx) {
+  if (idx < 0 || idx >= (int)NFORMATS) return PROXY_TO_DYNAMIC;
+  return convert<ExecSpace>(A, (formats_e)idx);
+}
+
+// impl/Coo/Serial/Morpheus_Sort_Impl.hpp:109-186
+template <class ExecSpace, class ValueType>
+void sort_by_row_and_column(CooMatrix<ValueType>& A) {
+  Impl::require_gb300<ExecSpace>();
+  mgb_coo d = A.desc();
+  Impl::check(Impl::Conv<ValueType>::sort(&d), "sort_by_row_and_column<GB300>");
+}
+template <class ExecSpace, class ValueType>
+bool is_sorted(const CooMatrix<ValueType>& A) {
+  Impl::require_gb300<ExecSpace>();
+  mgb_coo d = A.desc();
+  int sorted = 0;
+  Impl::check(mgb_coo_is_sorted(&d, &sorted, nullptr), "is_sorted<GB300>");
+  return sorted != 0;
 }
 
 }  // namespace Morpheus

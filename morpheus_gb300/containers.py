@@ -343,10 +343,11 @@ class DynamicMatrix(_Matrix):
 
     def activate(self, fmt) -> None:
         """core/src/Morpheus_DynamicMatrix.hpp:409-442: switch to an EMPTY
-        container of the new format (no data is converted).  An index past the
-        last format leaves the matrix unchanged."""
+        container of the new format (no data is converted).  Activating the
+        format that is already active, or an index past the last format,
+        leaves the matrix unchanged."""
         fmt = int(fmt)
-        if fmt < 0 or fmt >= NFORMATS:
+        if fmt < 0 or fmt >= NFORMATS or fmt == self.active_index():
             return
         self._set(_CLASSES[fmt](dtype=self.dtype, device=self.device))
 

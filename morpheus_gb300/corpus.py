@@ -133,17 +133,30 @@ def generate(seed: int, device="cuda") -> tuple[CsrMatrix, dict]:
     return A, desc
 
 
-def time_spmv(M, x: torch.Tensor, y: torch.Tensor, reps: int = 10, warmup: int = 2) -> float:
+def time_spmv(M, x: torch.Tensor, y: torch.Tensor, reps: int = 10, warmup: int = 2, replays: int = 3) -> float:
+    """Device time (ms) of one multiply: `reps` calls captured in one CUDA
+    graph, replayed `replays` times between CUDA events, so small matrices
+    are timed on the GPU rather than by the host's per-call overhead."""
     from .algorithms import multiply
-    for _ in range(warmup):
-        multiply(M, x, y)
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        for _ in range(warmup):  # also caches the CSR kernel choice outside the capture
+            multiply(M, x, y)
+    torch.cuda.current_stream().wait_stream(side)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        for _ in range(reps):
+            multiply(M, x, y)
+    g.replay()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
-    for _ in range(reps):
-        multiply(M, x, y)
+    for _ in range(replays):
+        g.replay()
     e1.record()
     torch.cuda.synchronize()
-    return e0.elapsed_time(e1) / reps
+    del g
+    return e0.elapsed_time(e1) / (reps * replays)
 
 
 def measure(A: CsrMatrix, reps: int = 10) -> np.ndarray:

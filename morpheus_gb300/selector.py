@@ -32,6 +32,24 @@ def _vp(t: torch.Tensor | None):
     return C.c_void_p(t.data_ptr() if t is not None else 0)
 
 
+def read_weights(path: str = DEFAULT_WEIGHTS) -> tuple[np.ndarray, np.ndarray, np.ndarray, dict]:
+    """(params, mu, sigma, metadata) of a weights file: MAGIC, u32 version,
+    u32 parameter count, u32 metadata length, mu[12], sigma[12],
+    params[5382] (little-endian float32), metadata (JSON)."""
+    import json
+    with open(path, "rb") as f:
+        if f.read(8) != MAGIC:
+            raise ValueError(f"{path}: not a selector weights file")
+        version, n, mlen = struct.unpack("<III", f.read(12))
+        if version != 1 or n != NPARAMS:
+            raise ValueError(f"{path}: unsupported version {version} / {n} parameters")
+        mu = np.frombuffer(f.read(4 * NFEATURES), "<f4").copy()
+        sigma = np.frombuffer(f.read(4 * NFEATURES), "<f4").copy()
+        params = np.frombuffer(f.read(4 * NPARAMS), "<f4").copy()
+        meta = json.loads(f.read(mlen).decode() or "{}")
+    return params, mu, sigma, meta
+
+
 class Selector:
     def __init__(self, params: np.ndarray, mu: np.ndarray, sigma: np.ndarray, device="cuda"):
         assert params.size == NPARAMS and mu.size == NFEATURES and sigma.size == NFEATURES
@@ -65,16 +83,8 @@ class Selector:
 
     @classmethod
     def load(cls, path: str = DEFAULT_WEIGHTS, device="cuda") -> "Selector":
-        with open(path, "rb") as f:
-            if f.read(8) != MAGIC:
-                raise ValueError(f"{path}: not a selector weights file")
-            version, n, mlen = struct.unpack("<III", f.read(12))
-            if version != 1 or n != NPARAMS:
-                raise ValueError(f"{path}: unsupported version {version} / {n} parameters")
-            mu = np.frombuffer(f.read(4 * NFEATURES), "<f4")
-            sigma = np.frombuffer(f.read(4 * NFEATURES), "<f4")
-            params = np.frombuffer(f.read(4 * NPARAMS), "<f4")
-        return cls(params.copy(), mu.copy(), sigma.copy(), device)
+        params, mu, sigma, _ = read_weights(path)
+        return cls(params, mu, sigma, device)
 
     # -- network ----------------------------------------------------------
     def logp(self, X: np.ndarray, feasible: np.ndarray | None = None) -> np.ndarray:
@@ -136,27 +146,43 @@ class Selector:
 
 # -- rule-based baseline (the method without the network) -----------------
 
-def rule_select(X: np.ndarray, feasible: np.ndarray, dia_fill_max: float, ell_fill_max: float) -> np.ndarray:
-    """DIA if its fill ratio <= t, else HYB if the ELL fill ratio <= p, else CSR."""
+RULE_GRID = {
+    "dia_fill_max": [0.0, 1.0, 1.1, 1.25, 1.5, 2.0, 3.0, 5.0],
+    "hdc_share_min": [0.5, 0.6, 0.7, 0.8, 0.9, 0.95, 0.99, 2.0],
+    "ell_fill_max": [0.0, 1.0, 1.05, 1.1, 1.25, 1.5, 2.0, 3.0],
+}
+
+
+def rule_select(X: np.ndarray, feasible: np.ndarray, dia_fill_max: float, hdc_share_min: float,
+                ell_fill_max: float) -> np.ndarray:
+    """The non-learned selector over the same GPU features: DIA if its fill
+    ratio <= dia_fill_max; else HDC if the true-diagonal share of the
+    nonzeros >= hdc_share_min; else ELL if its fill ratio <= ell_fill_max;
+    else CSR.  Infeasible formats are never chosen."""
     dia_fill = 2.0 ** X[:, 7]
+    share = X[:, 8]
     ell_fill = 2.0 ** X[:, 9]
     out = np.full(X.shape[0], 1)
-    hyb_ok = (ell_fill <= ell_fill_max) & (feasible[:, 4] > 0)
-    out[hyb_ok] = 4
+    ell_ok = (ell_fill <= ell_fill_max) & (feasible[:, 3] > 0)
+    out[ell_ok] = 3
+    hdc_ok = (share >= hdc_share_min) & (feasible[:, 5] > 0)
+    out[hdc_ok] = 5
     dia_ok = (dia_fill <= dia_fill_max) & (feasible[:, 2] > 0)
     out[dia_ok] = 2
     return out
 
 
-def tune_rule(X, feasible, times) -> tuple[float, float]:
-    """Grid-search the two thresholds for the lowest mean regret."""
-    best = (np.inf, 1.0, 1.0)
-    for t in [1.0, 1.1, 1.25, 1.5, 2.0, 3.0, 5.0, 10.0]:
-        for p in [1.0, 1.1, 1.25, 1.5, 2.0, 3.0, 5.0]:
-            r = regret(times, rule_select(X, feasible, t, p)).mean()
-            if r < best[0]:
-                best = (r, t, p)
-    return best[1], best[2]
+def tune_rule(X, feasible, times) -> dict:
+    """Grid-search the three thresholds for the lowest mean regret on the
+    training corpus (the rule's counterpart of training)."""
+    best, best_r = None, np.inf
+    for t in RULE_GRID["dia_fill_max"]:
+        for h in RULE_GRID["hdc_share_min"]:
+            for p in RULE_GRID["ell_fill_max"]:
+                r = regret(times, rule_select(X, feasible, t, h, p)).mean()
+                if r < best_r:
+                    best, best_r = {"dia_fill_max": t, "hdc_share_min": h, "ell_fill_max": p}, r
+    return best
 
 
 def regret(times: np.ndarray, choice: np.ndarray) -> np.ndarray:

@@ -7,8 +7,8 @@ Builds the synthetic corpus (morpheus_gb300/corpus.py: every format timed
 with CUDA events), trains the 12 -> 64 -> 64 -> 6 network with the project's
 own gradient and Adam kernels, and evaluates on held-out seeds against
 exhaustive timing (regret), against CSR-only, and against the rule-based
-selector (DIA if its fill ratio <= t, else HYB if the ELL fill ratio <= p,
-else CSR; t and p tuned on the training set).
+selector (DIA / HDC / ELL / CSR by three feature thresholds tuned on the
+training set, selector.rule_select).
 """
 from __future__ import annotations
 
@@ -39,7 +39,7 @@ def main(argv=None):
     te = corpus.build(args.test, seed0=1_000_000, reps=args.reps, log=print)
     t_corpus = time.time() - t0
     if args.corpus_out:
-        np.savez(args.corpus_out, Xtr=tr["X"], Ftr=tr["feasible"], Ttr=tr["times"], Xte=te["X"],
+        np.savez_compressed(args.corpus_out, Xtr=tr["X"], Ftr=tr["feasible"], Ttr=tr["times"], Xte=te["X"],
                  Fte=te["feasible"], Tte=te["times"])
 
     mu, sigma = tr["X"].mean(0), tr["X"].std(0) + 1e-3
@@ -49,8 +49,8 @@ def main(argv=None):
     t_train = time.time() - t1
 
     pred = sel.predict(te["X"], te["feasible"])
-    t, p = selector.tune_rule(tr["X"], tr["feasible"], tr["times"])
-    rule = selector.rule_select(te["X"], te["feasible"], t, p)
+    thr = selector.tune_rule(tr["X"], tr["feasible"], tr["times"])
+    rule = selector.rule_select(te["X"], te["feasible"], **thr)
     csr_only = np.full(len(pred), 1)
     names = ["COO", "CSR", "DIA", "ELL", "HYB", "HDC"]
     report = {
@@ -65,7 +65,7 @@ def main(argv=None):
                      "seconds": t_train, "train_accuracy": float(np.mean(
                          sel.predict(tr["X"], tr["feasible"]) == tr["labels"]))},
         "test": {"learned": selector.evaluate(te["times"], pred),
-                 "rule_based": dict(selector.evaluate(te["times"], rule), dia_fill_max=t, ell_fill_max=p),
+                 "rule_based": dict(selector.evaluate(te["times"], rule), **thr),
                  "csr_only": selector.evaluate(te["times"], csr_only)},
     }
     sel.save(args.out, {"report": report["test"], "corpus": report["corpus"]["train"]})

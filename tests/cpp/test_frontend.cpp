@@ -1,0 +1,379 @@
+// test_frontend.cpp -- the C++17 front end (include/Morpheus_GB300.hpp) on the
+// GPU, checked against the CPU oracle (oracle/liboracle.so, test
+// infrastructure only).  The cases follow the reference's own tests:
+//
+//   multiply   core/tests/Test_Multiply.hpp:161-186,202-257 (banded matrices,
+//              diagonals {0, +-5k}, N in {10, 100, 1000}, every format,
+//              init and accumulate)
+//   convert    core/tests/Serial/Test_Convert.hpp and
+//              core/tests/Serial/Test_Convert_Dynamic.hpp:195-213
+//              (structures bit-exact with the Serial convert, in-place
+//              DynamicMatrix round trips, error codes)
+//   dot        core/tests/Test_Dot.hpp:74-87   (sum (i+1)(n-i))
+//   reduce     core/tests/Test_Reduce.hpp:74-81 (sum (i+1.5))
+//   waxpby     core/tests/Test_WAXPBY.hpp
+//
+// Build: g++ -std=c++17 -Iinclude -I<cuda>/include tests/cpp/test_frontend.cpp
+//        -Lmorpheus_gb300 -lmorpheus_gb300 -Loracle/_build -loracle -lcudart
+// Exit status 0 when every check passes; one line per failed check.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "Morpheus_GB300.hpp"
+
+extern "C" {
+void* orc_new(int fmt, int dtype);
+void orc_free(void* p);
+int orc_resize(void* p, const int64_t* s);
+int orc_shape(void* p, int64_t* s);
+int64_t orc_array(void* p, const char* name, void** out);
+int orc_convert(void* src, void* dst);
+int orc_convert_inplace(void* p, int fmt);
+int orc_sort_by_row_and_column(void* p);
+int orc_multiply(void* p, const void* x, void* y, int init, int threads);
+void orc_waxpby_f64(int64_t n, double a, const double* x, double b, const double* y, double* w);
+}
+
+namespace {
+
+int g_checks = 0, g_failed = 0;
+
+void expect(bool ok, const std::string& what) {
+  ++g_checks;
+  if (!ok) {
+    ++g_failed;
+    std::printf("FAIL: %s\n", what.c_str());
+  }
+}
+
+template <class T> constexpr int dtype_code() { return std::is_same_v<T, double> ? 0 : 1; }
+template <class T> const char* tname() { return std::is_same_v<T, double> ? "double" : "float"; }
+
+// Host CSR of the reference's banded test matrix: diagonals 0 and +-k*freq,
+// values U[-2, 2] (never 0) from a seeded generator of this file.
+template <class T>
+struct HostCsr {
+  int64_t n = 0;
+  std::vector<int32_t> ro, ci;
+  std::vector<T> v;
+};
+
+template <class T>
+HostCsr<T> banded(int64_t n, int64_t freq, unsigned seed) {
+  HostCsr<T> h;
+  h.n = n;
+  std::mt19937_64 rng(seed);
+  std::uniform_real_distribution<double> U(-2.0, 2.0);
+  h.ro.push_back(0);
+  for (int64_t i = 0; i < n; i++) {
+    for (int64_t j = 0; j < n; j++) {
+      const int64_t d = j - i;
+      if (d % freq == 0) {
+        double val = U(rng);
+        if (val == 0.0) val = 1.0;
+        h.ci.push_back((int32_t)j);
+        h.v.push_back((T)val);
+      }
+    }
+    h.ro.push_back((int32_t)h.ci.size());
+  }
+  return h;
+}
+
+template <class T>
+std::vector<T> host_vector(int64_t n, unsigned seed) {
+  std::mt19937_64 rng(seed);
+  std::uniform_real_distribution<double> U(-1.0, 1.0);
+  std::vector<T> x((size_t)n);
+  for (auto& e : x) e = (T)U(rng);
+  return x;
+}
+
+// ------------------------------------------------------------- oracle side
+struct Oracle {
+  void* h = nullptr;
+  Oracle(int fmt, int dtype) : h(orc_new(fmt, dtype)) {}
+  ~Oracle() { if (h) orc_free(h); }
+  Oracle(const Oracle&) = delete;
+  Oracle& operator=(const Oracle&) = delete;
+  template <class E>
+  std::vector<E> array(const char* name) const {
+    void* p = nullptr;
+    const int64_t n = orc_array(h, name, &p);
+    if (n < 0) return {};
+    const E* q = static_cast<const E*>(p);
+    return std::vector<E>(q, q + n);
+  }
+  template <class E>
+  void set(const char* name, const std::vector<E>& src) {
+    void* p = nullptr;
+    const int64_t n = orc_array(h, name, &p);
+    if (n == (int64_t)src.size() && n > 0) std::memcpy(p, src.data(), sizeof(E) * (size_t)n);
+  }
+  std::vector<int64_t> shape() const {
+    std::vector<int64_t> s(10);
+    orc_shape(h, s.data());
+    return s;
+  }
+};
+
+template <class T>
+void oracle_from_csr(Oracle& o, const HostCsr<T>& A) {
+  int64_t s[10] = {1, A.n, A.n, (int64_t)A.v.size(), 0, 0, 0, 0, 0, 0};
+  orc_resize(o.h, s);
+  o.set("row_offsets", A.ro);
+  o.set("column_indices", A.ci);
+  o.set("values", A.v);
+}
+
+template <class T>
+double rel_err(const std::vector<T>& y, const std::vector<T>& ref) {
+  double num = 0, den = 0;
+  for (size_t i = 0; i < y.size(); i++) {
+    const double d = (double)y[i] - (double)ref[i];
+    num += d * d;
+    den += (double)ref[i] * (double)ref[i];
+  }
+  return den > 0 ? std::sqrt(num / den) : std::sqrt(num);
+}
+
+template <class T> double tol() { return std::is_same_v<T, double> ? 1e-12 : 1e-5; }
+
+}  // namespace
+
+namespace {
+
+using Morpheus::GB300;
+
+// bit-exact comparison of a device container with the oracle's container
+template <class E>
+bool same(const std::vector<E>& a, const std::vector<E>& b) {
+  return a.size() == b.size() && (a.empty() || std::memcmp(a.data(), b.data(), sizeof(E) * a.size()) == 0);
+}
+
+template <class T>
+bool same_structure(const Morpheus::CooMatrix<T>& m, const Oracle& o, const std::string& p = "") {
+  return same(m.crow_indices().to_host(), o.array<int32_t>((p + "row_indices").c_str())) &&
+         same(m.ccolumn_indices().to_host(), o.array<int32_t>((p + "column_indices").c_str())) &&
+         same(m.cvalues().to_host(), o.array<T>((p + "values").c_str()));
+}
+template <class T>
+bool same_structure(const Morpheus::CsrMatrix<T>& m, const Oracle& o, const std::string& p = "") {
+  return same(m.crow_offsets().to_host(), o.array<int32_t>((p + "row_offsets").c_str())) &&
+         same(m.ccolumn_indices().to_host(), o.array<int32_t>((p + "column_indices").c_str())) &&
+         same(m.cvalues().to_host(), o.array<T>((p + "values").c_str()));
+}
+template <class T>
+bool same_structure(const Morpheus::DiaMatrix<T>& m, const Oracle& o, const std::string& p = "") {
+  return same(m.cdiagonal_offsets().to_host(), o.array<int32_t>((p + "diagonal_offsets").c_str())) &&
+         same(m.cvalues().to_host(), o.array<T>((p + "values").c_str()));
+}
+template <class T>
+bool same_structure(const Morpheus::EllMatrix<T>& m, const Oracle& o, const std::string& p = "") {
+  return same(m.ccolumn_indices().to_host(), o.array<int32_t>((p + "column_indices").c_str())) &&
+         same(m.cvalues().to_host(), o.array<T>((p + "values").c_str()));
+}
+template <class T>
+bool same_structure(const Morpheus::HybMatrix<T>& m, const Oracle& o) {
+  return same_structure(m.cell(), o, "ell.") && same_structure(m.ccoo(), o, "coo.");
+}
+template <class T>
+bool same_structure(const Morpheus::HdcMatrix<T>& m, const Oracle& o) {
+  return same_structure(m.cdia(), o, "dia.") && same_structure(m.ccsr(), o, "csr.");
+}
+template <class T>
+bool same_structure(const Morpheus::DynamicMatrix<T>& m, const Oracle& o) {
+  return std::visit([&](const auto& a) { return same_structure(a, o); }, m.const_formats());
+}
+
+const char* kFormat[] = {"COO", "CSR", "DIA", "ELL", "HYB", "HDC"};
+
+// Test_Multiply + Test_Convert_Dynamic: CSR -> every format in place on the
+// GPU, structure against the Serial convert, multiply against the Serial
+// multiply, then back to CSR.
+template <class T>
+void test_banded(int64_t n) {
+  const HostCsr<T> h = banded<T>(n, 5, (unsigned)n);
+  const std::string tag = std::string(tname<T>()) + " banded N=" + std::to_string(n);
+  const Morpheus::CsrMatrix<T> A(n, n, h.ro, h.ci, h.v);
+  const std::vector<T> xh = host_vector<T>(n, 1), y0 = host_vector<T>(n, 2);
+  const Morpheus::DenseVector<T> x(xh);
+  for (int f = 0; f < (int)Morpheus::NFORMATS; f++) {
+    const std::string ft = tag + " -> " + kFormat[f];
+    Oracle o(1, dtype_code<T>());
+    oracle_from_csr(o, h);
+    const int oc = orc_convert_inplace(o.h, f);
+
+    Morpheus::DynamicMatrix<T> dyn(A);
+    const Morpheus::conversion_error_e ec = Morpheus::convert<GB300>(dyn, f);
+    expect((int)ec == oc, ft + ": conversion_error_e " + std::to_string((int)ec) + " vs " + std::to_string(oc));
+    if (oc != Morpheus::CONV_SUCCESS) {
+      expect(dyn.active_index() == Morpheus::CSR_FORMAT, ft + ": source kept after a failed conversion");
+      continue;
+    }
+    expect(dyn.active_index() == f, ft + ": active format");
+    expect(same_structure(dyn, o), ft + ": structure bit-exact with the Serial convert");
+
+    for (int init = 1; init >= 0; init--) {
+      std::vector<T> ref = y0;
+      orc_multiply(o.h, xh.data(), ref.data(), init, 0);
+      Morpheus::DenseVector<T> y(y0);
+      if (init) Morpheus::multiply<GB300>(dyn, x, y);
+      else Morpheus::multiply<GB300>(dyn, x, y, false);
+      const double e = rel_err(y.to_host(), ref);
+      expect(e <= tol<T>(), ft + (init ? " multiply" : " multiply (accumulate)") + ": rel err " + std::to_string(e));
+    }
+
+    // back to CSR through the generic convert(src, dst)
+    Morpheus::CsrMatrix<T> back;
+    Morpheus::convert<GB300>(dyn, back);
+    Oracle ob(1, dtype_code<T>());
+    orc_convert(o.h, ob.h);
+    expect(same_structure(back, ob), ft + " -> CSR: structure bit-exact with the Serial convert");
+  }
+}
+
+// in-place convert refused by the fill tolerance leaves the data in place
+void test_convert_errors() {
+  const int64_t n = 2000;
+  HostCsr<double> h;
+  h.n = n;
+  std::mt19937_64 rng(7);
+  h.ro.push_back(0);
+  for (int64_t i = 0; i < n; i++) {  // diagonal + one random entry per row: ~n diagonals
+    const int32_t j = (int32_t)(rng() % n);
+    if (j < i) { h.ci.push_back(j); h.v.push_back(1.0); }
+    h.ci.push_back((int32_t)i); h.v.push_back(2.0);
+    if (j > i) { h.ci.push_back(j); h.v.push_back(1.0); }
+    h.ro.push_back((int32_t)h.ci.size());
+  }
+  Morpheus::DynamicMatrix<double> dyn(Morpheus::CsrMatrix<double>(n, n, h.ro, h.ci, h.v));
+  Oracle o(1, 0);
+  oracle_from_csr(o, h);
+  const int oc = orc_convert_inplace(o.h, Morpheus::DIA_FORMAT);
+  const auto ec = Morpheus::convert<GB300>(dyn, Morpheus::DIA_FORMAT);
+  expect(oc == Morpheus::PROXY_TO_DYNAMIC, "oracle refuses DIA for a scattered matrix");
+  expect(ec == Morpheus::PROXY_TO_DYNAMIC, "convert<GB300>(dyn, DIA) returns PROXY_TO_DYNAMIC");
+  expect(dyn.active_index() == Morpheus::CSR_FORMAT && dyn.nnnz() == (int64_t)h.v.size(),
+         "matrix unchanged after PROXY_TO_DYNAMIC");
+  expect(Morpheus::convert<GB300>(dyn, Morpheus::CSR_FORMAT) == Morpheus::CONV_SUCCESS, "same-format convert");
+
+  bool threw = false;
+  try {
+    Morpheus::DiaMatrix<double> d;
+    Morpheus::convert<GB300>(Morpheus::CsrMatrix<double>(n, n, h.ro, h.ci, h.v), d);
+  } catch (const Morpheus::FormatConversionException&) {
+    threw = true;
+  }
+  expect(threw, "convert<GB300>(csr, dia) throws FormatConversionException");
+
+  threw = false;
+  try {
+    Morpheus::DenseVector<double> x(10), y(10);
+    Morpheus::multiply<GB300>(dyn, x, y);
+  } catch (const Morpheus::InvalidInputException&) {
+    threw = true;
+  }
+  expect(threw, "multiply with short vectors throws InvalidInputException");
+}
+
+// DynamicMatrix::activate: empty container of the new format; the active
+// format or an index past the last one changes nothing
+void test_activate() {
+  const HostCsr<double> h = banded<double>(50, 5, 3);
+  Morpheus::DynamicMatrix<double> dyn(Morpheus::CsrMatrix<double>(50, 50, h.ro, h.ci, h.v));
+  dyn.activate(Morpheus::CSR_FORMAT);
+  expect(dyn.nnnz() == (int64_t)h.v.size(), "activate(active format) keeps the data");
+  dyn.activate(17);
+  expect(dyn.active_index() == Morpheus::CSR_FORMAT && dyn.nnnz() == (int64_t)h.v.size(),
+         "activate(index past the last format) is a no-op");
+  dyn.activate(Morpheus::ELL_FORMAT);
+  expect(dyn.active_index() == Morpheus::ELL_FORMAT && dyn.nrows() == 0 && dyn.nnnz() == 0,
+         "activate switches to an empty container");
+}
+
+// COO sort on the device against the Serial sort
+void test_sort() {
+  const int64_t n = 300, nnz = 5000;
+  std::mt19937_64 rng(11);
+  std::vector<int32_t> r(nnz), c(nnz);
+  std::vector<double> v(nnz);
+  for (int64_t k = 0; k < nnz; k++) {
+    r[k] = (int32_t)(rng() % n);
+    c[k] = (int32_t)(rng() % n);
+    v[k] = (double)(k + 1);
+  }
+  Morpheus::CooMatrix<double> A(n, n, r, c, v);
+  expect(!Morpheus::is_sorted<GB300>(A), "random COO is not sorted");
+  Morpheus::sort_by_row_and_column<GB300>(A);
+  expect(Morpheus::is_sorted<GB300>(A), "sorted after sort_by_row_and_column");
+  Oracle o(0, 0);
+  int64_t s[10] = {0, n, n, nnz, 0, 0, 0, 0, 0, 0};
+  orc_resize(o.h, s);
+  o.set("row_indices", r);
+  o.set("column_indices", c);
+  o.set("values", v);
+  orc_sort_by_row_and_column(o.h);
+  expect(same_structure(A, o), "device sort bit-exact with the Serial sort (stable on duplicates)");
+}
+
+template <class T>
+void test_vector_ops() {
+  const std::string tag = tname<T>();
+  for (int64_t n : {1, 1000, 100000}) {
+    std::vector<T> a((size_t)n), b((size_t)n), c((size_t)n);
+    for (int64_t i = 0; i < n; i++) {
+      a[i] = (T)(i + 1);
+      b[i] = (T)(n - i);
+      c[i] = (T)(i + 1.5);
+    }
+    const Morpheus::DenseVector<T> x(a), y(b), z(c);
+    // sum_{i<n} (i+1)(n-i) = n(n+1)(n+2)/6
+    const double dot_ref = (double)n * (n + 1) * (n + 2) / 6.0;
+    const double d = (double)Morpheus::dot<GB300>((size_t)n, x, y);
+    expect(std::fabs(d - dot_ref) <= (std::is_same_v<T, double> ? 0.0 : 1e-6 * dot_ref),
+           tag + " dot known answer n=" + std::to_string(n));
+    // sum_{i<n} (i+1.5) = n(n+2)/2
+    const double red_ref = (double)n * (n + 2) / 2.0;
+    const double s = (double)Morpheus::reduce<GB300>(z, (size_t)n);
+    expect(std::fabs(s - red_ref) <= (std::is_same_v<T, double> ? 0.0 : 1e-6 * red_ref),
+           tag + " reduce known answer n=" + std::to_string(n));
+  }
+  const int64_t n = 12345;
+  const std::vector<T> a = host_vector<T>(n, 5), b = host_vector<T>(n, 6);
+  Morpheus::DenseVector<T> x(a), y(b), w(n);
+  Morpheus::waxpby<GB300>((size_t)n, (T)0.75, x, (T)-1.25, y, w);
+  const std::vector<T> wh = w.to_host();
+  bool ok = true;
+  for (int64_t i = 0; i < n; i++) {
+    const T ref = (T)0.75 * a[i] + (T)-1.25 * b[i];
+    if (std::fabs((double)wh[i] - (double)ref) > 4 * std::numeric_limits<T>::epsilon() * (std::fabs((double)ref) + 1))
+      ok = false;
+  }
+  expect(ok, tag + " waxpby");
+}
+
+}  // namespace
+
+int main() {
+  try {
+    for (int64_t n : {10, 100, 1000}) {
+      test_banded<double>(n);
+      test_banded<float>(n);
+    }
+    test_convert_errors();
+    test_activate();
+    test_sort();
+    test_vector_ops<double>();
+    test_vector_ops<float>();
+  } catch (const std::exception& e) {
+    std::printf("FAIL: unexpected exception: %s\n", e.what());
+    return 2;
+  }
+  std::printf("%d checks, %d failed\n", g_checks, g_failed);
+  return g_failed == 0 ? 0 : 1;
+}

@@ -1,0 +1,81 @@
+"""What the trained selector gains over the methods without it.
+
+tests/golden/selector_corpus.npz holds the features, feasibility masks and
+measured per-format SpMV times (CUDA-graph replays on a GB300) of the 2,000
+training and 400 held-out corpus matrices; morpheus_gb300/selector_weights.bin
+is the network trained on the training part.  Both were written by one run of
+
+    python -m morpheus_gb300.selector_train --train 2000 --test 400 \\
+        --out morpheus_gb300/selector_weights.bin \\
+        --corpus-out tests/golden/selector_corpus.npz
+
+On the held-out matrices the learned choice must stay within 10 % of the
+exhaustive best time on average (mean regret), be >= 1.5x faster than CSR
+only (geometric mean), and beat the rule-based selector whose thresholds are
+tuned on the same training matrices.  The CPU test runs the network through
+the FP64 oracle; the GPU test through the library's forward kernel.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from morpheus_gb300 import selector
+from oracle import mlp_oracle
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CORPUS = os.path.join(ROOT, "tests", "golden", "selector_corpus.npz")
+
+
+@pytest.fixture(scope="module")
+def corpus():
+    d = np.load(CORPUS)
+    return {k: d[k] for k in d.files}
+
+
+def _oracle_predict(X, F):
+    params, mu, sigma, _ = selector.read_weights()
+    p = mlp_oracle.forward(params, mu, np.maximum(sigma, 1e-6), X, F)["p"]
+    return np.argmax(p, axis=1)
+
+
+def _check_gain(choice, c):
+    learned = selector.evaluate(c["Tte"], choice)
+    thr = selector.tune_rule(c["Xtr"], c["Ftr"], c["Ttr"])
+    rule = selector.evaluate(c["Tte"], selector.rule_select(c["Xte"], c["Fte"], **thr))
+    assert learned["mean_regret"] <= 0.10, learned
+    assert learned["geomean_speedup_vs_csr"] >= 1.5, learned
+    assert learned["mean_regret"] < rule["mean_regret"], (learned, rule)
+    assert learned["geomean_speedup_vs_csr"] > rule["geomean_speedup_vs_csr"], (learned, rule)
+    return learned, rule
+
+
+def test_corpus_fixture_shape(corpus):
+    assert corpus["Xtr"].shape == (2000, 12) and corpus["Xte"].shape == (400, 12)
+    assert corpus["Ttr"].shape == (2000, 6) and corpus["Tte"].shape == (400, 6)
+    # CSR and COO always exist; a time is infinite exactly where the format is refused
+    for T, F in ((corpus["Ttr"], corpus["Ftr"]), (corpus["Tte"], corpus["Fte"])):
+        assert np.all(np.isfinite(T[:, :2]))
+        assert np.array_equal(np.isfinite(T), F > 0)
+
+
+def test_learned_selector_gain_oracle_forward(corpus):
+    choice = _oracle_predict(corpus["Xte"], corpus["Fte"])
+    assert np.all(corpus["Fte"][np.arange(len(choice)), choice] > 0)  # never an infeasible format
+    _check_gain(choice, corpus)
+
+
+def test_weights_metadata_matches_fixture(corpus):
+    """The report stored with the weights is what the fixture reproduces."""
+    _, _, _, meta = selector.read_weights()
+    learned = selector.evaluate(corpus["Tte"], _oracle_predict(corpus["Xte"], corpus["Fte"]))
+    assert learned["mean_regret"] == pytest.approx(meta["report"]["learned"]["mean_regret"], abs=0.01)
+
+
+@pytest.mark.gpu
+def test_learned_selector_gain_gpu_forward(cuda, corpus):
+    sel = selector.Selector.load()
+    choice = sel.predict(corpus["Xte"], corpus["Fte"])
+    agree = np.mean(choice == _oracle_predict(corpus["Xte"], corpus["Fte"]))
+    assert agree >= 0.99, agree
+    _check_gain(choice, corpus)
