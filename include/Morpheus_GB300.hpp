@@ -21,6 +21,7 @@
 
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdint>
 #include <stdexcept>
 #include <string>
@@ -747,6 +748,136 @@ bool is_sorted(const CooMatrix<ValueType>& A) {
   int sorted = 0;
   Impl::check(mgb_coo_is_sorted(&d, &sorted, nullptr), "is_sorted<GB300>");
   return sorted != 0;
+}
+
+// ------------------------------------------------------------ analytics ---
+// core/src/Morpheus_MatrixAnalytics.hpp:49-261 on the device.  CSR and COO
+// are counted directly; other formats go through COO first.
+namespace Impl {
+template <class T>
+void count_rows(const CsrMatrix<T>& A, int32_t* out, bool init) {
+  mgb_csr d = A.desc();
+  check(mgb_count_nnz_per_row_csr(&d, out, init, nullptr), "count_nnz_per_row<GB300>");
+}
+template <class T>
+void count_rows(const CooMatrix<T>& A, int32_t* out, bool init) {
+  mgb_coo d = A.desc();
+  check(mgb_count_nnz_per_row_coo(&d, out, init, nullptr), "count_nnz_per_row<GB300>");
+}
+template <class M>
+void count_rows(const M& A, int32_t* out, bool init) { count_rows(to_coo(A), out, init); }
+template <class T>
+void count_rows(const DynamicMatrix<T>& A, int32_t* out, bool init) {
+  std::visit([&](const auto& m) { count_rows(m, out, init); }, A.const_formats());
+}
+template <class T>
+void count_diags(const CsrMatrix<T>& A, int32_t* out, bool init) {
+  mgb_csr d = A.desc();
+  check(mgb_count_nnz_per_diagonal_csr(&d, out, init, nullptr), "count_nnz_per_diagonal<GB300>");
+}
+template <class T>
+void count_diags(const CooMatrix<T>& A, int32_t* out, bool init) {
+  mgb_coo d = A.desc();
+  check(mgb_count_nnz_per_diagonal_coo(&d, out, init, nullptr), "count_nnz_per_diagonal<GB300>");
+}
+template <class M>
+void count_diags(const M& A, int32_t* out, bool init) { count_diags(to_coo(A), out, init); }
+template <class T>
+void count_diags(const DynamicMatrix<T>& A, int32_t* out, bool init) {
+  std::visit([&](const auto& m) { count_diags(m, out, init); }, A.const_formats());
+}
+inline int64_t count_above(const DenseVector<int32_t>& v, int32_t threshold) {
+  int64_t c = 0;
+  check(mgb_count_nnz_vector(v.data(), (int64_t)v.size(), threshold, &c, nullptr), "count_nnz<GB300>");
+  return c;
+}
+template <class Matrix>
+std::vector<int32_t> row_lengths(const Matrix& A) {
+  DenseVector<int32_t> v((size_t)A.nrows(), 0);
+  count_rows(A, v.data(), true);
+  return v.to_host();
+}
+}  // namespace Impl
+
+template <class Matrix>
+int64_t number_of_rows(const Matrix& A) { return A.nrows(); }
+template <class Matrix>
+int64_t number_of_columns(const Matrix& A) { return A.ncols(); }
+template <class Matrix>
+int64_t number_of_nnz(const Matrix& A) { return A.nnnz(); }
+template <class Matrix>
+double average_nnnz(const Matrix& A) { return (double)A.nnnz() / (double)A.nrows(); }
+template <class Matrix>
+double density(const Matrix& A) { return (double)A.nnnz() / ((double)A.nrows() * (double)A.ncols()); }
+
+template <class ExecSpace, class Matrix>
+void count_nnz_per_row(const Matrix& A, DenseVector<int32_t>& nnz_per_row, const bool init = true) {
+  Impl::require_gb300<ExecSpace>();
+  if ((int64_t)nnz_per_row.size() < A.nrows()) throw InvalidInputException("count_nnz_per_row: vector too short");
+  Impl::count_rows(A, nnz_per_row.data(), init);
+}
+
+template <class ExecSpace, class Matrix>
+void count_nnz_per_diagonal(const Matrix& A, DenseVector<int32_t>& nnz_per_diagonal, const bool init = true) {
+  Impl::require_gb300<ExecSpace>();
+  if ((int64_t)nnz_per_diagonal.size() < A.nrows() + A.ncols() - 1)
+    throw InvalidInputException("count_nnz_per_diagonal: vector too short");
+  Impl::count_diags(A, nnz_per_diagonal.data(), init);
+}
+
+// entries of a count vector that are > threshold and != 0
+// (core/src/Morpheus_VectorAnalytics.hpp:124)
+template <class ExecSpace>
+int64_t count_nnz(const DenseVector<int32_t>& vec, int32_t threshold = 0) {
+  Impl::require_gb300<ExecSpace>();
+  return Impl::count_above(vec, threshold);
+}
+
+template <class ExecSpace, class Matrix>
+int64_t max_nnnz(const Matrix& A) {
+  Impl::require_gb300<ExecSpace>();
+  int64_t m = 0;
+  for (int32_t v : Impl::row_lengths(A)) m = v > m ? v : m;
+  return m;
+}
+
+template <class ExecSpace, class Matrix>
+int64_t min_nnnz(const Matrix& A) {
+  Impl::require_gb300<ExecSpace>();
+  const std::vector<int32_t> l = Impl::row_lengths(A);
+  int64_t m = l.empty() ? 0 : l[0];
+  for (int32_t v : l) m = v < m ? v : m;
+  return m;
+}
+
+// Standard deviation of the row lengths about the true mean, as a double
+// (the reference returns it truncated to an integer, about the integer mean
+// nnz / nrows, core/src/Morpheus_MatrixAnalytics.hpp:177-193).
+template <class ExecSpace, class Matrix>
+double std_nnnz(const Matrix& A) {
+  Impl::require_gb300<ExecSpace>();
+  const std::vector<int32_t> l = Impl::row_lengths(A);
+  if (l.empty()) return 0.0;
+  const double mean = (double)A.nnnz() / (double)l.size();
+  double acc = 0.0;
+  for (int32_t v : l) acc += ((double)v - mean) * ((double)v - mean);
+  return std::sqrt(acc / (double)l.size());
+}
+
+template <class ExecSpace, class Matrix>
+int64_t count_diagonals(const Matrix& A) {
+  Impl::require_gb300<ExecSpace>();
+  DenseVector<int32_t> v((size_t)(A.nrows() + A.ncols() - 1), 0);
+  Impl::count_diags(A, v.data(), true);
+  return Impl::count_above(v, 0);
+}
+
+template <class ExecSpace, class Matrix>
+int64_t count_true_diagonals(const Matrix& A, int32_t threshold) {
+  Impl::require_gb300<ExecSpace>();
+  DenseVector<int32_t> v((size_t)(A.nrows() + A.ncols() - 1), 0);
+  Impl::count_diags(A, v.data(), true);
+  return Impl::count_above(v, threshold);
 }
 
 }  // namespace Morpheus

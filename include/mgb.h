@@ -207,6 +207,22 @@ int mgb_waxpby_f32(int64_t n, float alpha, const float* x, float beta, const flo
  * Synchronises the stream. */
 int mgb_analytics_csr(const mgb_csr* A, double* out14, void* stream);
 
+/* Per-row and per-diagonal nonzero counts into device int32 vectors
+ * (count_nnz_per_row / count_nnz_per_diagonal,
+ * core/src/Morpheus_MatrixAnalytics.hpp:112-124,206-218): out has nrows
+ * entries, resp. nrows + ncols - 1 with diagonal d = column - row at
+ * index d + nrows - 1.  init != 0 zeroes out first, else counts are added.
+ * Asynchronous. */
+int mgb_count_nnz_per_row_csr(const mgb_csr* A, int32_t* out, int init, void* stream);
+int mgb_count_nnz_per_row_coo(const mgb_coo* A, int32_t* out, int init, void* stream);
+int mgb_count_nnz_per_diagonal_csr(const mgb_csr* A, int32_t* out, int init, void* stream);
+int mgb_count_nnz_per_diagonal_coo(const mgb_coo* A, int32_t* out, int init, void* stream);
+/* Number of entries of a device int32 vector that are > threshold and != 0
+ * (count_nnz, core/src/Morpheus_VectorAnalytics.hpp:124); with the
+ * per-diagonal counts it gives count_diagonals (threshold 0) and
+ * count_true_diagonals(A, threshold).  Synchronises the stream. */
+int mgb_count_nnz_vector(const int32_t* v, int64_t n, int32_t threshold, int64_t* count, void* stream);
+
 /* The format selector's 12 input features (host floats) and the feasibility
  * mask of the six formats (host bytes, may be NULL); no reference counterpart
  * (the reference's format choice is the --morpheus-format flag,

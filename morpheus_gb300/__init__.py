@@ -11,6 +11,7 @@ from .containers import (COO_FORMAT, CSR_FORMAT, DIA_FORMAT, ELL_FORMAT, HDC_FOR
                          CSR_ROWS, CSR_SEGMENTS, INVALID_INDEX, NFORMATS, CooMatrix, CsrMatrix, DiaMatrix, DynamicMatrix,
                          EllMatrix, HdcMatrix, HybMatrix, conversion_error_e, formats_e, get_pad_size,
                          matrix_from_host, matrix_to_host)
+from .matrix_market import read_matrix_market_file, write_matrix_market_file
 from .exceptions import (AllocationException, BadArgumentException, CudaException,
                          FormatConversionException, InvalidInputException, IOException,
                          MorpheusException, NotImplementedException, RuntimeException,
@@ -23,6 +24,7 @@ __all__ = [
     "formats_e", "conversion_error_e", "get_pad_size", "matrix_from_host", "matrix_to_host",
     "COO_FORMAT", "CSR_FORMAT", "DIA_FORMAT", "ELL_FORMAT", "HYB_FORMAT", "HDC_FORMAT", "NFORMATS",
     "INVALID_INDEX", "CSR_SEGMENTS", "CSR_ROWS",
+    "read_matrix_market_file", "write_matrix_market_file",
     "MorpheusException", "NotImplementedException", "FormatConversionException",
     "InvalidInputException", "RuntimeException", "IOException", "CudaException",
     "TimeoutException", "BadArgumentException", "AllocationException",

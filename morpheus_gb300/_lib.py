@@ -75,6 +75,11 @@ _SIGS["mgb_csr_choose_kernel"] = (C.c_int, [C.POINTER(Csr), C.POINTER(C.c_int), 
 for _dt in ("f64", "f32"):
     _SIGS[f"mgb_spmv_csr_variant_{_dt}"] = (C.c_int, [C.POINTER(Csr), vp, vp, C.c_int, C.c_int, vp])
 _SIGS["mgb_analytics_csr"] = (C.c_int, [C.POINTER(Csr), C.POINTER(C.c_double), vp])
+_SIGS["mgb_count_nnz_per_row_csr"] = (C.c_int, [C.POINTER(Csr), vp, C.c_int, vp])
+_SIGS["mgb_count_nnz_per_row_coo"] = (C.c_int, [C.POINTER(Coo), vp, C.c_int, vp])
+_SIGS["mgb_count_nnz_per_diagonal_csr"] = (C.c_int, [C.POINTER(Csr), vp, C.c_int, vp])
+_SIGS["mgb_count_nnz_per_diagonal_coo"] = (C.c_int, [C.POINTER(Coo), vp, C.c_int, vp])
+_SIGS["mgb_count_nnz_vector"] = (C.c_int, [vp, i64, C.c_int32, C.POINTER(i64), vp])
 _SIGS["mgb_features_csr"] = (C.c_int, [C.POINTER(Csr), C.POINTER(C.c_float), C.POINTER(C.c_uint8), vp])
 _SIGS["mgb_mlp_num_params"] = (C.c_int, [])
 _SIGS["mgb_mlp_forward_f32"] = (C.c_int, [vp, vp, vp, vp, vp, i64, vp, vp])

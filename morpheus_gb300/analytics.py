@@ -6,10 +6,12 @@ from __future__ import annotations
 import ctypes as C
 
 import numpy as np
+import torch
 
 from . import _lib
 from .algorithms import _stream_handle
-from .containers import CSR_FORMAT, CsrMatrix, DynamicMatrix, _Matrix
+from .containers import COO_FORMAT, CSR_FORMAT, CsrMatrix, DynamicMatrix, _Matrix
+from .exceptions import InvalidInputException
 
 NFEATURES = 12
 FEATURE_NAMES = ["log2_nrows", "log2_nnz", "mean_row", "cv_row", "log2_max_row", "min_row", "log2_ndiags",
@@ -51,5 +53,58 @@ def density(A) -> float: return analyze(A)["density"]
 def max_nnnz(A) -> int: return int(analyze(A)["max_nnnz"])
 def min_nnnz(A) -> int: return int(analyze(A)["min_nnnz"])
 def std_nnnz(A) -> float: return analyze(A)["std_nnnz"]
-def count_diagonals(A) -> int: return int(analyze(A)["count_diagonals"])
-def count_true_diagonals(A) -> int: return int(analyze(A)["count_true_diagonals"])
+
+
+def _csr_or_coo(A: _Matrix):
+    if isinstance(A, DynamicMatrix):
+        A = A.active()
+    if A.FORMAT in (CSR_FORMAT, COO_FORMAT):
+        return A
+    from .convert import to_coo
+    return to_coo(A)
+
+
+def _counts(A: _Matrix, what: str, n: int, out, init: bool, stream) -> torch.Tensor:
+    M = _csr_or_coo(A)
+    if out is None:
+        out = torch.zeros(n, dtype=torch.int32, device=M.device)
+        init = True
+    if out.dtype != torch.int32 or out.numel() < n or not out.is_contiguous() or out.device.type != "cuda":
+        raise InvalidInputException(f"{what}: out must be a contiguous CUDA int32 vector of {n} entries")
+    fmt = "csr" if M.FORMAT == CSR_FORMAT else "coo"
+    d = M._desc()
+    _lib.call(f"mgb_count_nnz_per_{what}_{fmt}", C.byref(d), C.c_void_p(out.data_ptr()), 1 if init else 0,
+              _stream_handle(stream))
+    return out
+
+
+def count_nnz_per_row(A: _Matrix, out: torch.Tensor | None = None, init: bool = True, stream=None) -> torch.Tensor:
+    """core/src/Morpheus_MatrixAnalytics.hpp:112-124: out[i] (+)= entries of row i."""
+    return _counts(A, "row", A.nrows(), out, init, stream)
+
+
+def count_nnz_per_diagonal(A: _Matrix, out: torch.Tensor | None = None, init: bool = True,
+                           stream=None) -> torch.Tensor:
+    """core/src/Morpheus_MatrixAnalytics.hpp:206-218: out[c - r + nrows - 1] (+)= 1."""
+    return _counts(A, "diagonal", A.nrows() + A.ncols() - 1, out, init, stream)
+
+
+def count_nnz(vec: torch.Tensor, threshold: int = 0, stream=None) -> int:
+    """core/src/Morpheus_VectorAnalytics.hpp:124: entries > threshold and != 0."""
+    if vec.dtype != torch.int32 or not vec.is_contiguous() or vec.device.type != "cuda":
+        raise InvalidInputException("count_nnz: a contiguous CUDA int32 vector is required")
+    out = C.c_int64()
+    _lib.call("mgb_count_nnz_vector", C.c_void_p(vec.data_ptr()), vec.numel(), int(threshold), C.byref(out),
+              _stream_handle(stream))
+    return out.value
+
+
+def count_diagonals(A: _Matrix) -> int:
+    """core/src/Morpheus_MatrixAnalytics.hpp:220-243"""
+    return count_nnz(count_nnz_per_diagonal(A), 0)
+
+
+def count_true_diagonals(A: _Matrix, threshold: int) -> int:
+    """core/src/Morpheus_MatrixAnalytics.hpp:245-261: diagonals with more than
+    `threshold` entries."""
+    return count_nnz(count_nnz_per_diagonal(A), threshold)

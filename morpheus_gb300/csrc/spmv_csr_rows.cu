@@ -5,8 +5,9 @@
 // user sets MATOPT_SHORT_ROWS (impl/Csr/Cuda/Morpheus_Multiply_Impl.hpp:59-92).
 // Here the choice is measured: mgb_csr_choose_kernel reads the row lengths
 // once and picks
-//   MGB_CSR_ROWS     when the longest row is <= 64 and <= 1.5 x mean + 2
-//                    (stencils, banded matrices, FEM meshes), else
+//   MGB_CSR_ROWS     when 32 rows of the longest length fit one staged tile
+//                    (longest row <= 28) and the longest row is <= 1.5 x
+//                    mean + 2 (stencils, banded matrices, FEM meshes), else
 //   MGB_CSR_SEGMENTS the lane-segment kernel of spmv_csr.cu (any structure).
 //
 // Row-tile kernel: one warp owns 32 consecutive rows.  The tile's entries are
@@ -110,7 +111,7 @@ int choose(const mgb_csr* A, int* variant, cudaStream_t s) {
   cudaFreeAsync(d, s);
   if (e != cudaSuccess) return record_cuda_error(e);
   const double mean = (double)A->nnz / (double)A->nrows;
-  if (mx <= 64 && (double)mx <= 1.5 * mean + 2.0) *variant = MGB_CSR_ROWS;
+  if (32 * mx <= ROWS_TILE_MAX && (double)mx <= 1.5 * mean + 2.0) *variant = MGB_CSR_ROWS;
   return MGB_SUCCESS;
 }
 

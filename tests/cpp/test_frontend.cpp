@@ -239,7 +239,7 @@ void test_banded(int64_t n) {
 
 // in-place convert refused by the fill tolerance leaves the data in place
 void test_convert_errors() {
-  const int64_t n = 2000;
+  const int64_t n = 20000;  // ~n diagonals: N * ndiags > 1e8 and fill > 10, so DIA is refused
   HostCsr<double> h;
   h.n = n;
   std::mt19937_64 rng(7);

@@ -141,3 +141,39 @@ def test_auto_format_switch(cuda):
         assert np.allclose(y.cpu().numpy(), ref, rtol=1e-12, atol=1e-12)
     finally:
         selector._DEFAULT = None
+
+
+@pytest.mark.parametrize("case", ["golden", "power_law", "stencil", "nonsquare"])
+@pytest.mark.parametrize("fmt", ["CSR", "COO", "HYB"])
+def test_count_nnz_per_row_and_diagonal(cuda, case, fmt):
+    """count_nnz_per_row / count_nnz_per_diagonal / count_diagonals /
+    count_true_diagonals against the oracle's per-diagonal count and host
+    per-row lengths, on CSR, COO and (through COO) HYB containers."""
+    if case == "golden":
+        A = golden()["CSR"]
+    elif case == "power_law":
+        A = gen.power_law(20000, seed=31)
+    elif case == "stencil":
+        A = gen.stencil_27pt(14, seed=32)
+    else:
+        A = gen.random_csr(300, 1100, 0.02, seed=33)
+    om = O.OracleMatrix.from_host(A)
+    host = om.convert(FORMATS_IDX[fmt]).to_host()
+    M = mgb.matrix_from_host(host, device="cuda")
+    lens = np.diff(A["row_offsets"].astype(np.int64))
+    diag = om.convert(O.COO).count_nnz_per_diagonal()
+    rows = analytics.count_nnz_per_row(M)
+    assert np.array_equal(rows.cpu().numpy(), lens)
+    d = analytics.count_nnz_per_diagonal(M)
+    assert np.array_equal(d.cpu().numpy(), diag)
+    # init=False accumulates into the given vector
+    analytics.count_nnz_per_diagonal(M, out=d, init=False)
+    assert np.array_equal(d.cpu().numpy(), 2 * diag)
+    analytics.count_nnz_per_row(M, out=rows, init=False)
+    assert np.array_equal(rows.cpu().numpy(), 2 * lens)
+    assert analytics.count_diagonals(M) == np.count_nonzero(diag)
+    for thr in (0, 1, 5, int(0.2 * A["nrows"])):
+        assert analytics.count_true_diagonals(M, thr) == np.count_nonzero(diag > thr)
+
+
+FORMATS_IDX = {"COO": 0, "CSR": 1, "DIA": 2, "ELL": 3, "HYB": 4, "HDC": 5}
