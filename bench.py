@@ -50,16 +50,23 @@ def peaks():
 # workloads
 # --------------------------------------------------------------------------
 
-def build_workload(name: str, fmt: str, dtype, seed: int):
+DEFAULT_SIZE = {"power_law": 2_000_000, "stencil27": 160, "laplacian": 256}
+
+
+def build_workload(name: str, fmt: str, dtype, seed: int, size: int | None = None):
+    """size: rows of the power-law matrix, or the grid edge of the stencil /
+    Laplacian (defaults: the benchmark configurations; smaller sizes are for
+    profiler captures)."""
     from morpheus_gb300 import generators as gen
+    n = size or DEFAULT_SIZE.get(name, 0)
     if name == "power_law":
-        A = gen.power_law(2_000_000, seed=seed, dtype=dtype)
+        A = gen.power_law(n, seed=seed, dtype=dtype)
     elif name == "stencil27":
-        A = gen.stencil_27pt(160, seed=seed, dtype=dtype)
+        A = gen.stencil_27pt(n, seed=seed, dtype=dtype)
         if fmt == "hdc":
             A = gen.add_offband(A, 0.01, seed=seed + 1)
     elif name == "laplacian":
-        A = gen.laplacian_2d(256, dtype=dtype)
+        A = gen.laplacian_2d(n, dtype=dtype)
     else:
         raise SystemExit(f"unknown workload {name}")
     if fmt == "csr":
@@ -206,7 +213,7 @@ def run_reference(args, rank: int):
               "nnz": sum(m["nnz"] for m in mats)}
         sample_desc = f"first {len(sample)} of {len(mats)} matrices per step, one OpenMP multiply each"
     else:
-        A, hm = build_workload(args.workload, args.format, dtype, seed=0)
+        A, hm = build_workload(args.workload, args.format, dtype, seed=0, size=args.size)
         nbytes = algorithmic_bytes(hm, vbytes)
         x = np.random.default_rng(1).uniform(-1, 1, hm["ncols"]).astype(dtype)
         om = O.OracleMatrix.from_host(hm)
@@ -244,7 +251,8 @@ def config_dict(args, hm):
             "nrows": hm["nrows"], "ncols": hm["ncols"], "nnz": hm["nnz"],
             "l2": "inputs larger than L2 (no flush needed)" if args.workload != "laplacian"
             else "L2 flushed between steps (256 MB scratch write)",
-            "parallelism": f"replicas x{args.gpus}"}
+            "parallelism": f"replicas x{args.gpus}",
+            **({"size": args.size} if getattr(args, "size", None) else {})}
 
 
 # --------------------------------------------------------------------------
@@ -264,7 +272,7 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
     dtype = np.float64 if args.dtype == "f64" else np.float32
     tdtype = torch.float64 if args.dtype == "f64" else torch.float32
     vbytes = np.dtype(dtype).itemsize
-    A, hm = build_workload(args.workload, args.format, dtype, seed=rank)
+    A, hm = build_workload(args.workload, args.format, dtype, seed=rank, size=args.size)
     nbytes = algorithmic_bytes(hm, vbytes)
     M = mgb.matrix_from_host(hm, device=dev)
     x_np = np.random.default_rng(1 + rank).uniform(-1, 1, hm["ncols"]).astype(dtype)
@@ -560,7 +568,7 @@ def launches_per_step(hm) -> int:
 def profile_traffic(args):
     """DRAM bytes per launch from the committed ncu summary, if one exists."""
     p = os.path.join(ROOT, "profiles", f"spmv_{args.format}_{args.workload}_{args.dtype}.md")
-    if not os.path.exists(p):
+    if args.size is not None or not os.path.exists(p):  # summaries describe the default sizes
         return None
     for line in open(p):
         if line.startswith("dram_bytes_per_launch:"):
@@ -579,6 +587,8 @@ def main():
     ap.add_argument("--impl", default="mgb", choices=["mgb", "reference"])
     ap.add_argument("--workload", default="power_law", choices=["power_law", "stencil27", "laplacian", "batched"])
     ap.add_argument("--batch", type=int, default=4096)
+    ap.add_argument("--size", type=int, default=None,
+                    help="power-law rows / stencil or Laplacian grid edge (default: the benchmark size)")
     ap.add_argument("--format", default="csr", choices=["csr", "coo", "dia", "ell", "hyb", "hdc"])
     ap.add_argument("--dtype", default="f64", choices=["f64", "f32"])
     ap.add_argument("--e2e-steps", type=int, default=10)

@@ -12,6 +12,8 @@
 //   dot        core/tests/Test_Dot.hpp:74-87   (sum (i+1)(n-i))
 //   reduce     core/tests/Test_Reduce.hpp:74-81 (sum (i+1.5))
 //   waxpby     core/tests/Test_WAXPBY.hpp
+//   I/O        core/tests/Test_MatrixMarket.hpp (files written by this program
+//              into the directory given as argv[1])
 //
 // Build: g++ -std=c++17 -Iinclude -I<cuda>/include tests/cpp/test_frontend.cpp
 //        -Lmorpheus_gb300 -lmorpheus_gb300 -Loracle/_build -loracle -lcudart
@@ -19,11 +21,13 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <fstream>
 #include <random>
 #include <string>
 #include <vector>
 
 #include "Morpheus_GB300.hpp"
+#include "Morpheus_GB300_MatrixMarket.hpp"
 
 extern "C" {
 void* orc_new(int fmt, int dtype);
@@ -357,9 +361,97 @@ void test_vector_ops() {
   expect(ok, tag + " waxpby");
 }
 
+template <class Exc>
+bool throws_on(const std::string& path, const std::string& text) {
+  {
+    std::ofstream f(path);
+    f << text;
+  }
+  try {
+    Morpheus::CooMatrix<double> A;
+    Morpheus::IO::read_matrix_market_file(A, path);
+  } catch (const Exc&) {
+    return true;
+  } catch (...) {
+    return false;
+  }
+  return false;
+}
+
+void test_matrix_market(const std::string& dir) {
+  const std::string f = dir + "/general.mtx";
+  {
+    std::ofstream o(f);
+    o << "%%MatrixMarket matrix coordinate real general\n% comment\n3 4 5\n3 4 -1.5\n1 1 1.25\n2 3 7\n"
+         "1 4 2.5e-3\n2 1 -0.5\n";
+  }
+  Morpheus::CooMatrix<double> A;
+  Morpheus::IO::read_matrix_market_file(A, f);
+  expect(A.nrows() == 3 && A.ncols() == 4 && A.nnnz() == 5, "mm: sizes");
+  expect(A.crow_indices().to_host() == std::vector<int32_t>({0, 0, 1, 1, 2}) &&
+             A.ccolumn_indices().to_host() == std::vector<int32_t>({0, 3, 0, 2, 3}) &&
+             A.cvalues().to_host() == std::vector<double>({1.25, 2.5e-3, -0.5, 7.0, -1.5}),
+         "mm: general real file sorted, base 0");
+
+  const std::string s = dir + "/sym.mtx";
+  {
+    std::ofstream o(s);
+    o << "%%MatrixMarket matrix coordinate pattern symmetric\n3 3 2\n2 1\n3 3\n";
+  }
+  Morpheus::DynamicMatrix<double> dyn(Morpheus::CooMatrix<double>{});
+  Morpheus::IO::read_matrix_market_file(dyn, s);
+  const auto& B = std::get<Morpheus::CooMatrix<double>>(dyn.const_formats());
+  expect(B.crow_indices().to_host() == std::vector<int32_t>({0, 1, 2}) &&
+             B.ccolumn_indices().to_host() == std::vector<int32_t>({1, 0, 2}),
+         "mm: symmetric pattern expanded");
+
+  const std::string bad = dir + "/bad.mtx";
+  expect(throws_on<Morpheus::IOException>(bad, "%%MatrixMarket matrix coordinate real general symmetric\n1 1 0\n"),
+         "mm: banner with an extra word");
+  expect(throws_on<Morpheus::IOException>(bad, "%%MatrixMarket matrix coordinate real general\n2 2 1\n0 1 1\n"),
+         "mm: zero row index");
+  expect(throws_on<Morpheus::IOException>(bad, "%%MatrixMarket matrix coordinate real general\n2 2 1\n1 3 1\n"),
+         "mm: column index past ncols");
+  expect(throws_on<Morpheus::IOException>(bad, "%%MatrixMarket matrix coordinate real general\n2 2 3\n1 1 1\n"),
+         "mm: unexpected EOF");
+  expect(throws_on<Morpheus::NotImplementedException>(bad,
+                                                      "%%MatrixMarket matrix coordinate complex general\n1 1 1\n1 1 1 0\n"),
+         "mm: complex");
+  expect(throws_on<Morpheus::NotImplementedException>(bad,
+                                                      "%%MatrixMarket matrix coordinate real hermitian\n1 1 1\n1 1 1\n"),
+         "mm: hermitian");
+
+  bool threw = false;
+  try {
+    Morpheus::DynamicMatrix<double> d(Morpheus::CsrMatrix<double>{});
+    Morpheus::IO::read_matrix_market_file(d, f);
+  } catch (const Morpheus::RuntimeException&) {
+    threw = true;
+  }
+  expect(threw, "mm: DynamicMatrix must be in COO");
+
+  // write -> read is bit-exact
+  const HostCsr<double> h = banded<double>(300, 7, 9);
+  Morpheus::CooMatrix<double> C;
+  Morpheus::convert<GB300>(Morpheus::CsrMatrix<double>(300, 300, h.ro, h.ci, h.v), C);
+  Morpheus::IO::write_matrix_market_file(C, dir + "/w.mtx");
+  Morpheus::CooMatrix<double> D;
+  Morpheus::IO::read_matrix_market_file(D, dir + "/w.mtx");
+  expect(D.crow_indices().to_host() == C.crow_indices().to_host() &&
+             D.ccolumn_indices().to_host() == C.ccolumn_indices().to_host() &&
+             D.cvalues().to_host() == C.cvalues().to_host(),
+         "mm: write -> read round trip bit-exact");
+  const Morpheus::DenseVector<float> x(host_vector<float>(33, 3));
+  Morpheus::IO::write_matrix_market_file(x, dir + "/x.mtx");
+  Morpheus::DenseVector<float> z;
+  Morpheus::IO::read_matrix_market_file(z, dir + "/x.mtx");
+  expect(z.to_host() == x.to_host(), "mm: vector round trip bit-exact");
+}
+
 }  // namespace
 
-int main() {
+int main(int argc, char** argv) {
+  const std::string dir = argc > 1 ? argv[1] : ".";
   try {
     for (int64_t n : {10, 100, 1000}) {
       test_banded<double>(n);
@@ -370,6 +462,7 @@ int main() {
     test_sort();
     test_vector_ops<double>();
     test_vector_ops<float>();
+    test_matrix_market(dir);
   } catch (const std::exception& e) {
     std::printf("FAIL: unexpected exception: %s\n", e.what());
     return 2;
