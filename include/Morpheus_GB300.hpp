@@ -880,6 +880,62 @@ int64_t count_true_diagonals(const Matrix& A, int32_t threshold) {
   return Impl::count_above(v, threshold);
 }
 
+// ------------------------------------------------------- solver steps ---
+// Fused steps of an iterative solver and a device-resident CG (mgb.h, no
+// reference counterpart).
+namespace Impl {
+template <class T> struct SolverAbi;
+template <> struct SolverAbi<double> {
+  static int spmv_dot(const mgb_csr* a, const double* x, double* y, int i, int v, double* d) {
+    return mgb_spmv_dot_csr_f64(a, x, y, i, v, d, nullptr);
+  }
+  static int cg(const mgb_csr* a, int v, const double* b, double* x, int64_t m, double t, int64_t* it, double* r) {
+    return mgb_cg_csr_f64(a, v, b, x, m, t, it, r, nullptr);
+  }
+};
+template <> struct SolverAbi<float> {
+  static int spmv_dot(const mgb_csr* a, const float* x, float* y, int i, int v, float* d) {
+    return mgb_spmv_dot_csr_f32(a, x, y, i, v, d, nullptr);
+  }
+  static int cg(const mgb_csr* a, int v, const float* b, float* x, int64_t m, double t, int64_t* it, double* r) {
+    return mgb_cg_csr_f32(a, v, b, x, m, t, it, r, nullptr);
+  }
+};
+}  // namespace Impl
+
+// y = A*x (init) or y += A*x, and returns x . y, in one pass over A.
+template <class ExecSpace, class T>
+T multiply_dot(const CsrMatrix<T>& A, const DenseVector<T>& x, DenseVector<T>& y, const bool init = true) {
+  Impl::require_gb300<ExecSpace>();
+  if ((int64_t)x.size() < A.ncols() || (int64_t)y.size() < A.nrows())
+    throw InvalidInputException("multiply_dot: vector sizes do not match the matrix");
+  DenseVector<T> d(1);
+  mgb_csr desc = A.desc();
+  Impl::check(Impl::SolverAbi<T>::spmv_dot(&desc, x.data(), y.data(), init, A.kernel_variant(), d.data()),
+              "multiply_dot<GB300>");
+  return d.to_host()[0];
+}
+
+struct CgResult {
+  int64_t iterations;
+  double relative_residual;  // sqrt(r.r / b.b) of the CG recurrence
+};
+
+// Conjugate gradients for an SPD CSR matrix; x holds the initial guess and
+// receives the solution.  Throws RuntimeException if the matrix is not SPD.
+template <class ExecSpace, class T>
+CgResult cg(const CsrMatrix<T>& A, const DenseVector<T>& b, DenseVector<T>& x, int64_t max_iters, double rtol) {
+  Impl::require_gb300<ExecSpace>();
+  if (A.nrows() != A.ncols() || (int64_t)b.size() < A.nrows() || (int64_t)x.size() < A.nrows())
+    throw InvalidInputException("cg: needs a square matrix and vectors of its size");
+  CgResult r{0, 0.0};
+  mgb_csr desc = A.desc();
+  Impl::check(Impl::SolverAbi<T>::cg(&desc, A.kernel_variant(), b.data(), x.data(), max_iters, rtol, &r.iterations,
+                                     &r.relative_residual),
+              "cg<GB300>");
+  return r;
+}
+
 }  // namespace Morpheus
 
 #endif  // MORPHEUS_GB300_HPP

@@ -348,6 +348,37 @@ int mgb_coo_sort_by_row_and_column_f32(mgb_coo* A, void* stream);
 /* impl/Coo/Serial/Morpheus_Sort_Impl.hpp:166-186; *sorted = 1 or 0 */
 int mgb_coo_is_sorted(const mgb_coo* A, int* sorted, void* stream);
 
+/* ---- fused solver steps (no reference counterpart) -----------------------
+ * The steps either side of SpMV in an iterative solver, fused into the pass
+ * that produces their input; a CG written on the reference's multiply / dot /
+ * waxpby (core/src/Morpheus_{Multiply,Dot,WAXPBY}.hpp) reads those vectors
+ * again.  Results are deterministic (fixed-order partial sums).
+ *
+ * y = A*x (init) or y += A*x, and *dot = x[0..nrows) . y, with the CSR kernel
+ * `variant` (mgb_csr_choose_kernel); dot is a DEVICE pointer; needs
+ * nrows <= ncols.  Asynchronous. */
+int mgb_spmv_dot_csr_f64(const mgb_csr* A, const double* x, double* y, int init, int variant, double* dot,
+                         void* stream);
+int mgb_spmv_dot_csr_f32(const mgb_csr* A, const float* x, float* y, int init, int variant, float* dot,
+                         void* stream);
+/* w = alpha*x + beta*y and *dot = w . w (device pointer).  Asynchronous. */
+int mgb_waxpby_dot_f64(int64_t n, double alpha, const double* x, double beta, const double* y, double* w,
+                       double* dot, void* stream);
+int mgb_waxpby_dot_f32(int64_t n, float alpha, const float* x, float beta, const float* y, float* w, float* dot,
+                       void* stream);
+/* Conjugate gradients for a symmetric positive definite CSR matrix: x (device,
+ * initial guess in, solution out) until ||r|| <= rtol * ||b|| or max_iters
+ * iterations.  alpha, beta and r.r stay on the device (five kernels per
+ * iteration: SpMV + p.Ap, alpha, x/r update + r.r, beta, p update), blocks
+ * of 16 iterations are one CUDA graph, and the host reads the state once per
+ * block.  *iters and *rel_residual (= sqrt(r.r / b.b) of the recurrence)
+ * are host pointers (may be NULL).  MGB_ERR_RUNTIME if p.Ap <= 0 (the matrix
+ * is not SPD).  Synchronises the stream. */
+int mgb_cg_csr_f64(const mgb_csr* A, int variant, const double* b, double* x, int64_t max_iters, double rtol,
+                   int64_t* iters, double* rel_residual, void* stream);
+int mgb_cg_csr_f32(const mgb_csr* A, int variant, const float* b, float* x, int64_t max_iters, double rtol,
+                   int64_t* iters, double* rel_residual, void* stream);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif

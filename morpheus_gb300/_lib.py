@@ -94,6 +94,11 @@ for _dt in ("f64", "f32"):
     _SIGS[f"mgb_spmv_batched_csr_{_dt}"] = (C.c_int, [vp, i64, C.c_int, vp, C.c_int, vp])
     _SIGS[f"mgb_spmv_batched_csr_autotune_{_dt}"] = (C.c_int, [vp, i64, vp, i64, C.c_int, C.POINTER(C.c_int),
                                                                C.POINTER(C.c_float), vp])
+for _dt, _ct in (("f64", C.c_double), ("f32", C.c_float)):
+    _SIGS[f"mgb_spmv_dot_csr_{_dt}"] = (C.c_int, [C.POINTER(Csr), vp, vp, C.c_int, C.c_int, vp, vp])
+    _SIGS[f"mgb_waxpby_dot_{_dt}"] = (C.c_int, [i64, _ct, vp, _ct, vp, vp, vp, vp])
+    _SIGS[f"mgb_cg_csr_{_dt}"] = (C.c_int, [C.POINTER(Csr), C.c_int, vp, vp, i64, C.c_double, C.POINTER(i64),
+                                            C.POINTER(C.c_double), vp])
 _SIGS["mgb_spmv_coo_f64_noalloc"] = (C.c_int, [C.POINTER(Coo), vp, vp, C.c_int, vp])
 _P = C.POINTER
 for _name, _s, _d in (("csr_to_coo", Csr, Coo), ("coo_to_csr", Coo, Csr), ("dia_to_coo", Dia, Coo),

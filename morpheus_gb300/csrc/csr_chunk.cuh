@@ -43,11 +43,17 @@ struct WarpStage {
   int32_t ro[CSR_RO_STAGE];
 };
 
+// Rows [begin, end) of one warp chunk.
+struct RowRange {
+  int64_t begin, end;
+};
+
 // Processes warp chunk `wc` of one CSR matrix: the rows whose first entry lies
 // in [wc*CHUNK, (wc+1)*CHUNK).  Chunks are whole rows, so every y entry is
-// written by exactly one warp.
+// written by exactly one warp.  Returns the chunk's rows (their y entries are
+// visible to the whole warp after a __syncwarp()).
 template <typename T, int64_t CHUNK, int SEG>
-__device__ __forceinline__ void csr_chunk(int64_t wc, int64_t nrows, int64_t ncols,
+__device__ __forceinline__ RowRange csr_chunk(int64_t wc, int64_t nrows, int64_t ncols,
                                           const int32_t* __restrict__ ro, const int32_t* __restrict__ ci,
                                           const T* __restrict__ va, const T* __restrict__ x,
                                           T* __restrict__ y, int init, WarpStage<T, SEG>& stg, int lane) {
@@ -61,7 +67,7 @@ __device__ __forceinline__ void csr_chunk(int64_t wc, int64_t nrows, int64_t nco
   int64_t r_end = warp_lower_bound(ro, r_begin, nrows + 1, s1, lane);
   if (r_begin > nrows) r_begin = nrows;
   if (r_end > nrows) r_end = nrows;
-  if (r_begin >= r_end) return;
+  if (r_begin >= r_end) return RowRange{r_begin, r_begin};
   const int64_t nr = r_end - r_begin;
   const bool staged = nr < CSR_RO_STAGE;  // offsets r_begin..r_end in smem
   __syncwarp();
@@ -75,7 +81,7 @@ __device__ __forceinline__ void csr_chunk(int64_t wc, int64_t nrows, int64_t nco
   if (E0 >= E1) {  // only empty rows
     if (init)
       for (int64_t r = r_begin + lane; r < r_end; r += 32) y[r] = T(0);
-    return;
+    return RowRange{r_begin, r_end};
   }
   const int64_t A0 = E0 & ~(int64_t)7;  // 32-byte aligned column segments
   int64_t KW = (E1 - A0 + 31) / 32;
@@ -169,6 +175,7 @@ __device__ __forceinline__ void csr_chunk(int64_t wc, int64_t nrows, int64_t nco
   const T vprev = __shfl_up_sync(0xffffffffu, cv, 1);
   const int64_t kprev = __shfl_up_sync(0xffffffffu, key, 1);
   if (hrow >= 0) y[hrow] = (lane > 0 && kprev == hrow) ? hval + vprev : hval;
+  return RowRange{r_begin, r_end};
 }
 
 }  // namespace csr

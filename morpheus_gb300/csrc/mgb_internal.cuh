@@ -58,8 +58,16 @@ template <typename T>
 int launch_ell(const mgb_ell* A, const T* x, T* y, int init, cudaStream_t s);
 template <typename T>
 int launch_coo(const mgb_coo* A, const T* x, T* y, int init, cudaStream_t s);
+// CSR SpMV with an explicit kernel (MGB_CSR_SEGMENTS / MGB_CSR_ROWS).  With
+// partials != nullptr the kernel also forms x[0..nrows) . y, one partial per
+// warp, *npartials of them; partials == nullptr with npartials != nullptr
+// only reports that count.
 template <typename T>
-int launch_csr_rows(const mgb_csr* A, const T* x, T* y, int init, cudaStream_t s);
+int launch_csr_dot(const mgb_csr* A, const T* x, T* y, int init, void* stream, int variant, T* partials,
+                   int64_t* npartials);
+template <typename T>
+int launch_csr_rows(const mgb_csr* A, const T* x, T* y, int init, cudaStream_t s, T* partials = nullptr,
+                    int64_t* npartials = nullptr);
 
 // Validation helpers for descriptors.
 inline bool bad_sizes(int64_t a, int64_t b, int64_t c) { return a < 0 || b < 0 || c < 0; }

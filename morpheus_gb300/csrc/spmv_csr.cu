@@ -38,22 +38,44 @@ namespace {
 
 constexpr int CSR_WARPS = 8;  // warps per CTA
 
-template <typename T>
+// DOT: also x[0..nrows) . y of the finished rows, one partial per warp in
+// partials[blockIdx.x * CSR_WARPS + warp] (the fused step of an iterative
+// solver; the matrix is square there).
+template <typename T, bool DOT>
 __global__ void __launch_bounds__(CSR_WARPS * 32, 3)
 spmv_csr_segments(int64_t nrows, int64_t ncols, int64_t nnz, int64_t nchunks,
                   const int32_t* __restrict__ ro, const int32_t* __restrict__ ci,
                   const T* __restrict__ va, const T* __restrict__ x,
-                  T* __restrict__ y, int init) {
+                  T* __restrict__ y, int init, T* __restrict__ partials) {
   __shared__ csr::WarpStage<T, csr::CSR_SEG> stage[CSR_WARPS];
   const int lane = threadIdx.x & 31;
   const int w = threadIdx.x >> 5;
+  T part = T(0);
   for (int64_t wc = (int64_t)blockIdx.x * CSR_WARPS + w; wc < nchunks;
-       wc += (int64_t)gridDim.x * CSR_WARPS)
-    csr::csr_chunk<T, csr::CSR_CHUNK, csr::CSR_SEG>(wc, nrows, ncols, ro, ci, va, x, y, init, stage[w], lane);
+       wc += (int64_t)gridDim.x * CSR_WARPS) {
+    const csr::RowRange rr =
+        csr::csr_chunk<T, csr::CSR_CHUNK, csr::CSR_SEG>(wc, nrows, ncols, ro, ci, va, x, y, init, stage[w], lane);
+    if (DOT) {
+      __syncwarp();  // the chunk's y entries, written by any lane, are visible to the warp
+      for (int64_t r = rr.begin + lane; r < rr.end; r += 32) part = fmadd(x[r], y[r], part);
+    }
+  }
+  if (DOT) {
+    part = warp_sum(part);
+    if (lane == 0) partials[(int64_t)blockIdx.x * CSR_WARPS + w] = part;
+  }
 }
 
 template <typename T>
 int launch_csr(const mgb_csr* A, const T* x, T* y, int init, void* stream, int variant = MGB_CSR_SEGMENTS) {
+  return launch_csr_dot<T>(A, x, y, init, stream, variant, nullptr, nullptr);
+}
+
+}  // namespace
+
+template <typename T>
+int launch_csr_dot(const mgb_csr* A, const T* x, T* y, int init, void* stream, int variant, T* partials,
+                   int64_t* npartials) {
   MGB_REQUIRE(A != nullptr, MGB_ERR_BAD_ARGUMENT);
   MGB_REQUIRE(!bad_sizes(A->nrows, A->ncols, A->nnz), MGB_ERR_BAD_ARGUMENT);
   MGB_REQUIRE(A->nnz < ((int64_t)1 << 31) - 4096, MGB_ERR_INVALID_INPUT);
@@ -61,20 +83,28 @@ int launch_csr(const mgb_csr* A, const T* x, T* y, int init, void* stream, int v
   if (A->nrows == 0) return MGB_SUCCESS;
   MGB_REQUIRE(A->row_offsets != nullptr && y != nullptr, MGB_ERR_BAD_ARGUMENT);
   MGB_REQUIRE(A->nnz == 0 || (A->column_indices && A->values && x), MGB_ERR_BAD_ARGUMENT);
-  if (variant == MGB_CSR_ROWS) return launch_csr_rows<T>(A, x, y, init, as_stream(stream));
+  if (variant == MGB_CSR_ROWS) return launch_csr_rows<T>(A, x, y, init, as_stream(stream), partials, npartials);
   // one extra chunk so rows whose first entry is at nnz (trailing empty rows)
   // always belong to some chunk
   const int64_t nchunks = A->nnz / csr::CSR_CHUNK + 1;
   int64_t blocks = (nchunks + CSR_WARPS - 1) / CSR_WARPS;
   if (blocks > 0x7fffffffLL) blocks = 0x7fffffffLL;
-  spmv_csr_segments<T><<<(unsigned)blocks, CSR_WARPS * 32, 0, as_stream(stream)>>>(
-      A->nrows, A->ncols, A->nnz, nchunks, A->row_offsets, A->column_indices,
-      static_cast<const T*>(A->values), x, y, init);
+  if (npartials) *npartials = blocks * CSR_WARPS;
+  if (npartials && !partials) return MGB_SUCCESS;
+  if (partials)
+    spmv_csr_segments<T, true><<<(unsigned)blocks, CSR_WARPS * 32, 0, as_stream(stream)>>>(
+        A->nrows, A->ncols, A->nnz, nchunks, A->row_offsets, A->column_indices,
+        static_cast<const T*>(A->values), x, y, init, partials);
+  else
+    spmv_csr_segments<T, false><<<(unsigned)blocks, CSR_WARPS * 32, 0, as_stream(stream)>>>(
+        A->nrows, A->ncols, A->nnz, nchunks, A->row_offsets, A->column_indices,
+        static_cast<const T*>(A->values), x, y, init, nullptr);
   MGB_LAUNCH_CHECK();
   return MGB_SUCCESS;
 }
+template int launch_csr_dot<double>(const mgb_csr*, const double*, double*, int, void*, int, double*, int64_t*);
+template int launch_csr_dot<float>(const mgb_csr*, const float*, float*, int, void*, int, float*, int64_t*);
 
-}  // namespace
 }  // namespace mgb
 
 extern "C" {

@@ -25,10 +25,13 @@ namespace {
 constexpr int ROWS_WARPS = 4;
 constexpr int ROWS_TILE_MAX = 896;  // 32 rows x 28 entries
 
-template <typename T>
+// DOT: also x[0..nrows) . y, one partial per warp in
+// partials[blockIdx.x * ROWS_WARPS + warp].
+template <typename T, bool DOT>
 __global__ void __launch_bounds__(ROWS_WARPS * 32, 5)
 spmv_csr_rowtile(int64_t nrows, int64_t ncols, const int32_t* __restrict__ ro, const int32_t* __restrict__ ci,
-                 const T* __restrict__ va, const T* __restrict__ x, T* __restrict__ y, int init) {
+                 const T* __restrict__ va, const T* __restrict__ x, T* __restrict__ y, int init,
+                 T* __restrict__ partials) {
   __shared__ T s_val[ROWS_WARPS][ROWS_TILE_MAX];
   __shared__ int32_t s_col[ROWS_WARPS][ROWS_TILE_MAX];
   const int lane = threadIdx.x & 31;
@@ -36,6 +39,7 @@ spmv_csr_rowtile(int64_t nrows, int64_t ncols, const int32_t* __restrict__ ro, c
   T* sv = s_val[w];
   int32_t* sc = s_col[w];
   const int64_t ntiles = (nrows + 31) >> 5;
+  T part = T(0);
   for (int64_t tile = (int64_t)blockIdx.x * ROWS_WARPS + w; tile < ntiles;
        tile += (int64_t)gridDim.x * ROWS_WARPS) {
     const int64_t r = (tile << 5) + lane;
@@ -66,7 +70,14 @@ spmv_csr_rowtile(int64_t nrows, int64_t ncols, const int32_t* __restrict__ ro, c
         }
       }
     }
-    if (valid) y[r] = acc;
+    if (valid) {
+      y[r] = acc;
+      if (DOT) part = fmadd(x[r], acc, part);
+    }
+  }
+  if (DOT) {
+    part = warp_sum(part);
+    if (lane == 0) partials[(int64_t)blockIdx.x * ROWS_WARPS + w] = part;
   }
 }
 
@@ -79,12 +90,20 @@ __global__ void row_shape_kernel(const int32_t* __restrict__ ro, int64_t nrows, 
 }
 
 template <typename T>
-int launch_rows(const mgb_csr* A, const T* x, T* y, int init, cudaStream_t s) {
+int launch_rows(const mgb_csr* A, const T* x, T* y, int init, cudaStream_t s, T* partials, int64_t* npartials) {
   const int64_t ntiles = (A->nrows + 31) / 32;
   int64_t blocks = (ntiles + ROWS_WARPS - 1) / ROWS_WARPS;
   if (blocks > 0x7fffffffLL) blocks = 0x7fffffffLL;
-  spmv_csr_rowtile<T><<<(unsigned)blocks, ROWS_WARPS * 32, 0, s>>>(
-      A->nrows, A->ncols, A->row_offsets, A->column_indices, static_cast<const T*>(A->values), x, y, init);
+  if (npartials) *npartials = blocks * ROWS_WARPS;
+  if (npartials && !partials) return MGB_SUCCESS;
+  if (partials)
+    spmv_csr_rowtile<T, true><<<(unsigned)blocks, ROWS_WARPS * 32, 0, s>>>(
+        A->nrows, A->ncols, A->row_offsets, A->column_indices, static_cast<const T*>(A->values), x, y, init,
+        partials);
+  else
+    spmv_csr_rowtile<T, false><<<(unsigned)blocks, ROWS_WARPS * 32, 0, s>>>(
+        A->nrows, A->ncols, A->row_offsets, A->column_indices, static_cast<const T*>(A->values), x, y, init,
+        nullptr);
   MGB_LAUNCH_CHECK();
   return MGB_SUCCESS;
 }
@@ -119,11 +138,11 @@ int choose(const mgb_csr* A, int* variant, cudaStream_t s) {
 
 // CSR SpMV entry with an explicit kernel choice (used by spmv_csr.cu too)
 template <typename T>
-int launch_csr_rows(const mgb_csr* A, const T* x, T* y, int init, cudaStream_t s) {
-  return launch_rows<T>(A, x, y, init, s);
+int launch_csr_rows(const mgb_csr* A, const T* x, T* y, int init, cudaStream_t s, T* partials, int64_t* npartials) {
+  return launch_rows<T>(A, x, y, init, s, partials, npartials);
 }
-template int launch_csr_rows<double>(const mgb_csr*, const double*, double*, int, cudaStream_t);
-template int launch_csr_rows<float>(const mgb_csr*, const float*, float*, int, cudaStream_t);
+template int launch_csr_rows<double>(const mgb_csr*, const double*, double*, int, cudaStream_t, double*, int64_t*);
+template int launch_csr_rows<float>(const mgb_csr*, const float*, float*, int, cudaStream_t, float*, int64_t*);
 
 }  // namespace mgb
 

@@ -448,6 +448,47 @@ void test_matrix_market(const std::string& dir) {
   expect(z.to_host() == x.to_host(), "mm: vector round trip bit-exact");
 }
 
+// fused SpMV + dot equals multiply + dot; CG solves an SPD system
+void test_solver() {
+  const int64_t n = 4000;
+  HostCsr<double> h;
+  h.n = n;
+  h.ro.push_back(0);
+  for (int64_t i = 0; i < n; i++) {  // symmetric, diagonally dominant: SPD
+    for (int64_t d : {-9, -1, 0, 1, 9}) {
+      const int64_t j = i + d;
+      if (j < 0 || j >= n) continue;
+      h.ci.push_back((int32_t)j);
+      h.v.push_back(d == 0 ? 4.5 : -1.0);
+    }
+    h.ro.push_back((int32_t)h.ci.size());
+  }
+  const Morpheus::CsrMatrix<double> A(n, n, h.ro, h.ci, h.v);
+  const std::vector<double> bh = host_vector<double>(n, 21);
+  const Morpheus::DenseVector<double> b(bh);
+  Morpheus::DenseVector<double> y(n), y2(n);
+  const double d = Morpheus::multiply_dot<GB300>(A, b, y);
+  Morpheus::multiply<GB300>(A, b, y2);
+  expect(y.to_host() == y2.to_host(), "multiply_dot: y bit-identical to multiply");
+  const double d2 = Morpheus::dot<GB300>((size_t)n, b, y2);
+  expect(std::fabs(d - d2) <= 1e-12 * std::fabs(d2), "multiply_dot: dot matches dot<GB300>");
+
+  Morpheus::DenseVector<double> x(n, 0.0);
+  const Morpheus::CgResult r = Morpheus::cg<GB300>(A, b, x, 1000, 1e-11);
+  expect(r.iterations > 0 && r.iterations < 1000 && r.relative_residual <= 1e-11, "cg converges");
+  Oracle o(1, 0);
+  oracle_from_csr(o, h);
+  std::vector<double> ax(n, 0.0);
+  const std::vector<double> xh = x.to_host();
+  orc_multiply(o.h, xh.data(), ax.data(), 1, 0);
+  double num = 0, den = 0;
+  for (int64_t i = 0; i < n; i++) {
+    num += (bh[i] - ax[i]) * (bh[i] - ax[i]);
+    den += bh[i] * bh[i];
+  }
+  expect(std::sqrt(num / den) <= 1e-9, "cg: true residual against the oracle multiply");
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -463,6 +504,7 @@ int main(int argc, char** argv) {
     test_vector_ops<double>();
     test_vector_ops<float>();
     test_matrix_market(dir);
+    test_solver();
   } catch (const std::exception& e) {
     std::printf("FAIL: unexpected exception: %s\n", e.what());
     return 2;
