@@ -48,21 +48,34 @@ struct RowRange {
   int64_t begin, end;
 };
 
+// x read through the read-only global path
+template <typename T>
+struct XGlobal {
+  const T* __restrict__ p;
+  __device__ __forceinline__ T operator()(int32_t c) const { return __ldg(p + c); }
+};
+// x staged in shared memory (p points into the kernel's shared array)
+template <typename T>
+struct XShared {
+  const T* p;
+  __device__ __forceinline__ T operator()(int32_t c) const { return p[c]; }
+};
+
 // Processes warp chunk `wc` of one CSR matrix: the rows whose first entry lies
-// in [wc*CHUNK, (wc+1)*CHUNK).  Chunks are whole rows, so every y entry is
+// in [wc*chunk, (wc+1)*chunk).  Chunks are whole rows, so every y entry is
 // written by exactly one warp.  Returns the chunk's rows (their y entries are
-// visible to the whole warp after a __syncwarp()).
-template <typename T, int64_t CHUNK, int SEG>
-__device__ __forceinline__ RowRange csr_chunk(int64_t wc, int64_t nrows, int64_t ncols,
-                                          const int32_t* __restrict__ ro, const int32_t* __restrict__ ci,
-                                          const T* __restrict__ va, const T* __restrict__ x,
-                                          T* __restrict__ y, int init, WarpStage<T, SEG>& stg, int lane) {
+// visible to the whole warp after a __syncwarp()).  xl(c) reads x[c].
+template <typename T, int SEG, typename XL>
+__device__ __forceinline__ RowRange csr_chunk_x(int64_t wc, int64_t chunk, int64_t nrows, int64_t ncols,
+                                                const int32_t* __restrict__ ro, const int32_t* __restrict__ ci,
+                                                const T* __restrict__ va, XL xl, T* __restrict__ y, int init,
+                                                WarpStage<T, SEG>& stg, int lane) {
   constexpr int CSR_PAD = SEG + 1;
   T* sv = stg.val;
   int32_t* sc = stg.col;
   int32_t* sro = stg.ro;
   // rows starting in [s0, s1)
-  const int64_t s0 = wc * CHUNK, s1 = s0 + CHUNK;
+  const int64_t s0 = wc * chunk, s1 = s0 + chunk;
   int64_t r_begin = warp_lower_bound(ro, 0, nrows + 1, s0, lane);
   int64_t r_end = warp_lower_bound(ro, r_begin, nrows + 1, s1, lane);
   if (r_begin > nrows) r_begin = nrows;
@@ -132,7 +145,7 @@ __device__ __forceinline__ RowRange csr_chunk(int64_t wc, int64_t nrows, int64_t
       const bool valid = e >= e_lo && e < lb;
       const int32_t c = sc[lane * CSR_PAD + k];
       v[k] = valid ? sv[lane * CSR_PAD + k] : T(0);
-      xv[k] = (valid && (uint64_t)(int64_t)c < (uint64_t)ncols) ? __ldg(x + c) : T(0);
+      xv[k] = (valid && (uint64_t)(int64_t)c < (uint64_t)ncols) ? xl(c) : T(0);
     }
 #pragma unroll
     for (int k = 0; k < SEG; k++) {
@@ -176,6 +189,14 @@ __device__ __forceinline__ RowRange csr_chunk(int64_t wc, int64_t nrows, int64_t
   const int64_t kprev = __shfl_up_sync(0xffffffffu, key, 1);
   if (hrow >= 0) y[hrow] = (lane > 0 && kprev == hrow) ? hval + vprev : hval;
   return RowRange{r_begin, r_end};
+}
+
+template <typename T, int64_t CHUNK, int SEG>
+__device__ __forceinline__ RowRange csr_chunk(int64_t wc, int64_t nrows, int64_t ncols,
+                                              const int32_t* __restrict__ ro, const int32_t* __restrict__ ci,
+                                              const T* __restrict__ va, const T* __restrict__ x,
+                                              T* __restrict__ y, int init, WarpStage<T, SEG>& stg, int lane) {
+  return csr_chunk_x<T, SEG>(wc, CHUNK, nrows, ncols, ro, ci, va, XGlobal<T>{x}, y, init, stg, lane);
 }
 
 }  // namespace csr

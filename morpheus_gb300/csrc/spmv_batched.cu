@@ -16,8 +16,13 @@
 //
 // Tunables (CHUNK nonzeros per warp = 32 x lane range, SEG = entries staged
 // per lane per step, the "vector width" of the staging loads) form six
-// configurations; mgb_spmv_batched_csr_autotune_* times each on the actual
-// batch with CUDA events and returns the fastest.
+// chunk-queue configurations.  Two more configurations give each CTA a whole
+// matrix at a time (largest first): the CTA copies the matrix's x into
+// shared memory (up to 64 KB) and its warps split the matrix into
+// nnz-balanced chunks, so the random x reads become shared-memory reads
+// instead of one L1TEX sector per nonzero (the unit that binds the
+// chunk-queue kernel).  mgb_spmv_batched_csr_autotune_* times every
+// configuration on the actual batch with CUDA events and returns the fastest.
 #include "csr_chunk.cuh"
 #include "primitives.cuh"
 
@@ -25,11 +30,17 @@ namespace mgb {
 namespace {
 
 constexpr int BAT_WARPS = 8;
-constexpr int BAT_NCONFIGS = 6;
-constexpr int64_t BAT_CHUNK[BAT_NCONFIGS] = {512, 1024, 2048, 4096, 1024, 2048};
-constexpr int BAT_SEG[BAT_NCONFIGS] = {8, 8, 8, 8, 4, 4};
-// workspace: int32 header[4] = {work counter, total chunks, planned config,
-// error flag}, then int32 prefix[nitems + 1]
+constexpr int BAT_NCONFIGS = 8;
+constexpr int BAT_FIRST_XS = 6;  // configurations >= this keep x in shared memory
+// chunk-queue configs: nonzeros per chunk; matrix-per-CTA configs: 0 (each
+// matrix is cut into 8 x BAT_XS_CPW chunks of at least 256 nonzeros)
+constexpr int64_t BAT_CHUNK[BAT_NCONFIGS] = {512, 1024, 2048, 4096, 1024, 2048, 0, 0};
+constexpr int BAT_SEG[BAT_NCONFIGS] = {8, 8, 8, 8, 4, 4, 8, 8};
+constexpr int BAT_XS_CPW[BAT_NCONFIGS] = {0, 0, 0, 0, 0, 0, 1, 2};  // chunks per warp
+constexpr int BAT_XS_BYTES = 64 * 1024;  // shared-memory copy of x (larger x: read from global)
+// workspace: int32 header[4] = {work counter, total work items, planned
+// config, error flag}, then int32[nitems + 1]: the chunk prefix (chunk-queue
+// configs) or the matrix order, largest nnz first (matrix-per-CTA configs)
 constexpr int BAT_HEADER = 4;
 
 __global__ void batch_chunk_counts(const mgb_csr_batch_item* __restrict__ items, int64_t n, int64_t chunk,
@@ -77,6 +88,75 @@ spmv_batched_csr(const mgb_csr_batch_item* __restrict__ items, int64_t nitems, i
   }
 }
 
+// One CTA per matrix at a time, x in shared memory (configs >= BAT_FIRST_XS).
+template <typename T, int CFG>
+__global__ void __launch_bounds__(BAT_WARPS * 32, 2)
+spmv_batched_csr_xs(const mgb_csr_batch_item* __restrict__ items, int64_t nitems, int32_t* ws, int init) {
+  constexpr int SEG = BAT_SEG[CFG];
+  constexpr int64_t CPW = BAT_XS_CPW[CFG];
+  constexpr int64_t XCAP = BAT_XS_BYTES / sizeof(T);
+  extern __shared__ __align__(16) unsigned char bat_smem[];
+  T* xs = reinterpret_cast<T*>(bat_smem);
+  csr::WarpStage<T, SEG>* stage = reinterpret_cast<csr::WarpStage<T, SEG>*>(bat_smem + BAT_XS_BYTES);
+  __shared__ int s_q;
+  const int lane = threadIdx.x & 31;
+  const int w = threadIdx.x >> 5;
+  if (ws[2] != CFG) {
+    if (threadIdx.x == 0) ws[3] = 1;
+    return;
+  }
+  const int32_t* __restrict__ order = ws + BAT_HEADER;
+  while (true) {
+    if (threadIdx.x == 0) s_q = atomicAdd(ws, 1);
+    __syncthreads();
+    const int q = s_q;
+    __syncthreads();  // every thread has read s_q before it is overwritten
+    if (q >= nitems) break;
+    const mgb_csr_batch_item it = items[__ldg(order + q)];
+    const T* xg = static_cast<const T*>(it.x);
+    const bool xin = it.ncols <= XCAP;
+    if (xin)
+      for (int64_t i = threadIdx.x; i < it.ncols; i += blockDim.x) xs[i] = __ldg(xg + i);
+    __syncthreads();
+    int64_t chunk = (it.nnz + BAT_WARPS * CPW - 1) / (BAT_WARPS * CPW);
+    chunk = (chunk + 255) / 256 * 256;
+    chunk = chunk < 256 ? 256 : (chunk > 4096 ? 4096 : chunk);
+    const int64_t nch = it.nnz / chunk + 1;
+    const T* va = static_cast<const T*>(it.values);
+    T* y = static_cast<T*>(it.y);
+    for (int64_t c = w; c < nch; c += BAT_WARPS) {
+      if (xin)
+        csr::csr_chunk_x<T, SEG>(c, chunk, it.nrows, it.ncols, it.row_offsets, it.column_indices, va,
+                                 csr::XShared<T>{xs}, y, init, stage[w], lane);
+      else
+        csr::csr_chunk_x<T, SEG>(c, chunk, it.nrows, it.ncols, it.row_offsets, it.column_indices, va,
+                                 csr::XGlobal<T>{xg}, y, init, stage[w], lane);
+    }
+    __syncthreads();  // x buffer is reused by the next matrix
+  }
+}
+
+// order keys: (INT32_MAX - nnz) << 32 | index, so an ascending sort puts the
+// largest matrices first (longest-processing-time-first scheduling)
+__global__ void batch_order_keys(const mgb_csr_batch_item* __restrict__ items, int64_t n, uint64_t* keys) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    int64_t z = items[i].nnz;
+    z = z < 0 ? 0 : (z > 0x7fffffffLL ? 0x7fffffffLL : z);
+    keys[i] = ((uint64_t)(0x7fffffffLL - z) << 32) | (uint64_t)i;
+  }
+}
+
+__global__ void batch_order_finish(const uint64_t* __restrict__ keys, int64_t n, int32_t* ws, int config) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    ws[BAT_HEADER + i] = (int32_t)(keys[i] & 0xffffffffu);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    ws[0] = 0;
+    ws[1] = (int32_t)n;
+    ws[2] = config;
+    ws[3] = 0;
+  }
+}
+
 int64_t workspace_bytes(int64_t nitems) { return sizeof(int32_t) * (BAT_HEADER + nitems + 1); }
 
 int plan(const mgb_csr_batch_item* items, int64_t nitems, int config, void* workspace, int64_t ws_bytes,
@@ -85,6 +165,25 @@ int plan(const mgb_csr_batch_item* items, int64_t nitems, int config, void* work
   MGB_REQUIRE(config >= 0 && config < BAT_NCONFIGS, MGB_ERR_BAD_ARGUMENT);
   MGB_REQUIRE(ws_bytes >= workspace_bytes(nitems), MGB_ERR_BAD_ARGUMENT);
   int32_t* ws = static_cast<int32_t*>(workspace);
+  MGB_REQUIRE(nitems < 0x7fffffffLL, MGB_ERR_INVALID_INPUT);
+  if (config >= BAT_FIRST_XS) {
+    prim::Scratch sc(s);
+    uint64_t* keys;
+    int32_t* seg;
+    MGB_SCRATCH(sc, keys, nitems);
+    MGB_SCRATCH(sc, seg, 2);
+    const int32_t hseg[2] = {0, (int32_t)nitems};
+    MGB_CUDA_CHECK(cudaMemcpyAsync(seg, hseg, sizeof(hseg), cudaMemcpyHostToDevice, s));
+    batch_order_keys<<<prim::blocks_for(nitems, 256), 256, 0, s>>>(items, nitems, keys);
+    MGB_LAUNCH_CHECK();
+    int st = prim::segmented_sort_u64(keys, seg, 1, nitems, s);
+    if (st) return st;
+    batch_order_finish<<<prim::blocks_for(nitems, 256), 256, 0, s>>>(keys, nitems, ws, config);
+    MGB_LAUNCH_CHECK();
+    // hseg is read by the copy before this function returns
+    MGB_CUDA_CHECK(cudaStreamSynchronize(s));
+    return MGB_SUCCESS;
+  }
   int32_t* counts;
   int64_t* d_total;
   prim::Scratch sc(s);
@@ -102,8 +201,21 @@ int plan(const mgb_csr_batch_item* items, int64_t nitems, int config, void* work
 
 template <typename T, int CFG>
 int launch_cfg(const mgb_csr_batch_item* items, int64_t nitems, int32_t* ws, int init, cudaStream_t s) {
-  const int blocks = num_sms() * 3;
-  spmv_batched_csr<T, CFG><<<blocks, BAT_WARPS * 32, 0, s>>>(items, nitems, ws, init);
+  if constexpr (CFG >= BAT_FIRST_XS) {
+    constexpr size_t smem = BAT_XS_BYTES + BAT_WARPS * sizeof(csr::WarpStage<T, BAT_SEG[CFG]>);
+    // set once per device (a function attribute, not a stream operation)
+    static bool attr_set[64] = {};
+    int dev = 0;
+    MGB_CUDA_CHECK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64 || !attr_set[dev]) {
+      MGB_CUDA_CHECK(cudaFuncSetAttribute(spmv_batched_csr_xs<T, CFG>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      if (dev >= 0 && dev < 64) attr_set[dev] = true;
+    }
+    spmv_batched_csr_xs<T, CFG><<<num_sms() * 2, BAT_WARPS * 32, smem, s>>>(items, nitems, ws, init);
+  } else {
+    spmv_batched_csr<T, CFG><<<num_sms() * 3, BAT_WARPS * 32, 0, s>>>(items, nitems, ws, init);
+  }
   MGB_LAUNCH_CHECK();
   return MGB_SUCCESS;
 }
@@ -121,7 +233,9 @@ int launch(const mgb_csr_batch_item* items, int64_t nitems, int config, void* wo
     case 2: return launch_cfg<T, 2>(items, nitems, ws, init, s);
     case 3: return launch_cfg<T, 3>(items, nitems, ws, init, s);
     case 4: return launch_cfg<T, 4>(items, nitems, ws, init, s);
-    default: return launch_cfg<T, 5>(items, nitems, ws, init, s);
+    case 5: return launch_cfg<T, 5>(items, nitems, ws, init, s);
+    case 6: return launch_cfg<T, 6>(items, nitems, ws, init, s);
+    default: return launch_cfg<T, 7>(items, nitems, ws, init, s);
   }
 }
 

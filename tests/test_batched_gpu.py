@@ -33,7 +33,7 @@ def check(mats, xs, ys, y0s, init, tol):
         assert rel_err(y.cpu().numpy(), ref) <= tol
 
 
-@pytest.mark.parametrize("config", range(6))
+@pytest.mark.parametrize("config", range(8))
 def test_every_config(cuda, config):
     mats, dev, xs, ys, _ = make_batch(60, seed=config)
     y0s = [y.cpu().numpy() for y in ys]
@@ -68,12 +68,37 @@ def test_autotune_and_graph_replay(cuda):
     check(mats, xs, ys, y0s, True, 1e-12)
 
 
+@pytest.mark.parametrize("config", [6, 7])
+def test_shared_x_configs_f32_and_wide_x(cuda, config):
+    """Matrix-per-CTA configurations keep x in shared memory up to 64 KB;
+    wider x (here 20,000 and 40,000 columns) is read from global memory."""
+    mats, dev, xs, ys, _ = make_batch(40, seed=20 + config, dtype=np.float32)
+    extra = gen.random_lengths_csr(300, 40000, np.full(300, 25), seed=9, dtype=np.float32)
+    mats.append(extra)
+    dev.append(mgb.matrix_from_host(extra))
+    xs.append(torch.from_numpy(gen.x_vector(40000, seed=4, dtype=np.float32)).cuda())
+    ys.append(torch.zeros(300, dtype=torch.float32, device="cuda"))
+    b = batched.CsrBatch(dev, xs, ys)
+    b.plan(config)
+    b.multiply(init=True)
+    torch.cuda.synchronize()
+    assert b.planned_ok()
+    for m, x, y in zip(mats, xs, ys):
+        ref = O.OracleMatrix.from_host({k: (v.astype(np.float64) if isinstance(v, np.ndarray) and v.dtype.kind == "f"
+                                            else v) for k, v in m.items()}).multiply(x.double().cpu().numpy())
+        scale = O.OracleMatrix.from_host({k: (np.abs(v).astype(np.float64) if isinstance(v, np.ndarray)
+                                              and v.dtype.kind == "f" else v) for k, v in m.items()}).multiply(
+            np.abs(x.double().cpu().numpy()))
+        err = np.linalg.norm(y.double().cpu().numpy() - ref) / max(np.linalg.norm(scale), 1e-300)
+        assert err <= 1e-5
+
+
 def test_config_mismatch_is_a_noop(cuda):
     mats, dev, xs, ys, _ = make_batch(10, seed=5)
     b = batched.CsrBatch(dev, xs, ys)
     b.plan(1)
     before = [y.clone() for y in ys]
-    b.config = 3  # launch a config the workspace was not planned for
+    b.config = 6  # launch a config the workspace was not planned for
     b.multiply()
     torch.cuda.synchronize()
     assert not b.planned_ok()
