@@ -421,6 +421,83 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
     print(json.dumps(line), flush=True)
 
 
+def run_gpu_cg(args, rank: int, world: int, local_rank: int):
+    """Conjugate gradients on a 2-D 5-point Laplacian (SPD, default 2048^2 grid,
+    N = 4.19 M, nnz = 21 M, CSR FP64): the device-resident fused CG
+    (mgb_cg_csr_f64: SpMV + p.Ap, x/r update + r.r, graph-captured blocks of
+    16 iterations) against the same recurrence composed of the library's
+    separate calls (multiply, dot, waxpby).  One step = one CG iteration;
+    `value` = fused iterations per second; the unfused rate is reported beside it."""
+    import torch
+    import morpheus_gb300 as mgb
+    from morpheus_gb300 import generators as gen
+    from morpheus_gb300 import solvers
+    dev = torch.device("cuda", local_rank)
+    torch.cuda.set_device(dev)
+    n = args.size or 2048
+    hm = gen.laplacian_2d(n)
+    A = mgb.matrix_from_host(hm, device=dev)
+    N = hm["nrows"]
+    b = torch.from_numpy(np.random.default_rng(3 + rank).uniform(-1, 1, N)).to(dev)
+    iters = max(args.steps, 16)
+    stream = torch.cuda.current_stream(dev)
+
+    def fused():
+        x = torch.zeros(N, dtype=torch.float64, device=dev)
+        it, _ = solvers.cg(A, b, x, max_iters=iters, rtol=0.0)
+        return it
+
+    def unfused():
+        # the same recurrence from the separate calls; dot returns a host scalar
+        x = torch.zeros(N, dtype=torch.float64, device=dev)
+        r = b.clone()
+        p = r.clone()
+        ap = torch.empty_like(r)
+        rr = mgb.dot(N, r, r)
+        for _ in range(iters):
+            mgb.multiply(A, p, ap)
+            alpha = rr / mgb.dot(N, p, ap)
+            mgb.waxpby(N, 1.0, x, alpha, p, x)
+            mgb.waxpby(N, 1.0, r, -alpha, ap, r)
+            rr_new = mgb.dot(N, r, r)
+            mgb.waxpby(N, 1.0, r, rr_new / rr, p, p)
+            rr = rr_new
+        return iters
+
+    for _ in range(max(1, args.warmup)):
+        fused()
+    unfused()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    time.sleep(0.3)
+    e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    e0.record(stream)
+    done = fused()
+    e1.record(stream)
+    unfused()
+    e2.record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    fused_ms = e0.elapsed_time(e1)
+    unfused_ms = e1.elapsed_time(e2)
+    spmv_bytes = algorithmic_bytes(hm, 8)
+    line = {
+        "metric": "CG iterations/s (fused device-resident CG)", "value": done / (fused_ms * 1e-3),
+        "unit": "iterations/s", "n_gpus": 1, "steps": done, "warmup": args.warmup,
+        "ms_per_step": fused_ms / done, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (2-D 5-point Laplacian, b uniform in [-1, 1])",
+        "config": {"workload": f"cg_laplacian_{n}x{n}_f64", "nrows": N, "nnz": hm["nnz"],
+                   "kernel_variant": A.kernel_variant()},
+        "unfused": {"value": iters / (unfused_ms * 1e-3), "unit": "iterations/s", "ms_per_step": unfused_ms / iters},
+        "speedup_of_fused": unfused_ms / fused_ms,
+        "spmv_share_bytes_per_iteration": spmv_bytes,
+        "clocks": clocks,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def run_gpu_batched(args, rank: int, world: int, local_rank: int):
     """4,096 independent FP64 CSR SpMVs per step in one autotuned persistent
     launch, replayed as a CUDA graph; baseline: the same SpMVs as separate
@@ -585,7 +662,7 @@ def main():
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="mgb", choices=["mgb", "reference"])
-    ap.add_argument("--workload", default="power_law", choices=["power_law", "stencil27", "laplacian", "batched"])
+    ap.add_argument("--workload", default="power_law", choices=["power_law", "stencil27", "laplacian", "batched", "cg"])
     ap.add_argument("--batch", type=int, default=4096)
     ap.add_argument("--size", type=int, default=None,
                     help="power-law rows / stencil or Laplacian grid edge (default: the benchmark size)")
@@ -608,6 +685,8 @@ def main():
     try:
         if args.workload == "batched":
             run_gpu_batched(args, rank, world, local_rank)
+        elif args.workload == "cg":
+            run_gpu_cg(args, rank, world, local_rank)
         else:
             run_gpu(args, rank, world, local_rank)
     finally:

@@ -27,8 +27,17 @@ namespace {
 constexpr int COO_WARPS = 8;
 constexpr int COO_SEG = 8;                  // entries per lane per staging step
 constexpr int COO_PAD = COO_SEG + 1;        // padded lane stride in shared memory
-constexpr int64_t COO_CHUNK = 2048;         // entries per warp chunk
-constexpr int COO_KW = (int)(COO_CHUNK / 32);  // entries per lane
+constexpr int64_t COO_CHUNK = 2048;         // entries per warp chunk (largest)
+
+// 2048 entries per chunk, halved (down to 256) while the matrix would give
+// fewer chunks than the GPU holds resident warps, so small matrices still
+// spread over every SM.
+inline int64_t coo_chunk_size(int64_t nnz) {
+  int64_t chunk = COO_CHUNK;
+  const int64_t resident = (int64_t)num_sms() * COO_WARPS * 3;
+  while (chunk > 256 && nnz / chunk < resident) chunk >>= 1;
+  return chunk;
+}
 
 template <typename T>
 __device__ __forceinline__ T gather_x(const T* __restrict__ x, int32_t c, int64_t ncols) {
@@ -37,7 +46,7 @@ __device__ __forceinline__ T gather_x(const T* __restrict__ x, int32_t c, int64_
 
 template <typename T>
 __global__ void __launch_bounds__(COO_WARPS * 32, 3)
-spmv_coo_segments(int64_t nrows, int64_t ncols, int64_t nnz, const int32_t* __restrict__ ri,
+spmv_coo_segments(int64_t nrows, int64_t ncols, int64_t nnz, int64_t chunk, const int32_t* __restrict__ ri,
                   const int32_t* __restrict__ ci, const T* __restrict__ va, const T* __restrict__ x,
                   T* __restrict__ y, int init, int32_t* __restrict__ carry_row, T* __restrict__ carry_val) {
   __shared__ T s_val[COO_WARPS][32 * COO_PAD];
@@ -49,12 +58,13 @@ spmv_coo_segments(int64_t nrows, int64_t ncols, int64_t nnz, const int32_t* __re
   int32_t* sc = s_col[w];
   int32_t* sr = s_row[w];
 
-  const int64_t nchunks = (nnz + COO_CHUNK - 1) / COO_CHUNK;
+  const int64_t nchunks = (nnz + chunk - 1) / chunk;
+  const int64_t KW = chunk / 32;  // entries per lane, a multiple of COO_SEG
   for (int64_t k = (int64_t)blockIdx.x * COO_WARPS + w; k < nchunks; k += (int64_t)gridDim.x * COO_WARPS) {
-    const int64_t base = k * COO_CHUNK;
-    const int64_t cend = min(base + COO_CHUNK, nnz);
-    const int64_t la = base + (int64_t)lane * COO_KW;
-    const int64_t lb = min(la + COO_KW, cend);
+    const int64_t base = k * chunk;
+    const int64_t cend = min(base + chunk, nnz);
+    const int64_t la = base + (int64_t)lane * KW;
+    const int64_t lb = min(la + KW, cend);
     const bool active = la < lb;
     const int64_t first_row = __ldg(ri + base);
     const int64_t last_row = __ldg(ri + cend - 1);
@@ -86,13 +96,13 @@ spmv_coo_segments(int64_t nrows, int64_t ncols, int64_t nnz, const int32_t* __re
     int64_t hrow = -1;
     T hval = T(0), acc = T(0);
 
-    for (int st = 0; st < COO_KW; st += COO_SEG) {
+    for (int64_t st = 0; st < KW; st += COO_SEG) {
       __syncwarp();
 #pragma unroll
       for (int q = 0; q < COO_SEG; q++) {
         const int f = q * 32 + lane;
         const int L = f / COO_SEG, j = f % COO_SEG;
-        const int64_t e = base + (int64_t)L * COO_KW + st + j;
+        const int64_t e = base + (int64_t)L * KW + st + j;
         const bool in = e < cend;
         sr[L * COO_PAD + j] = in ? ldg_stream(ri + e) : -1;
         sc[L * COO_PAD + j] = in ? ldg_stream(ci + e) : 0;
@@ -180,7 +190,8 @@ int launch_coo(const mgb_coo* A, const T* x, T* y, int init, cudaStream_t s) {
     return MGB_SUCCESS;
   }
   MGB_REQUIRE(A->row_indices && A->column_indices && A->values && x, MGB_ERR_BAD_ARGUMENT);
-  const int64_t nchunks = (A->nnz + COO_CHUNK - 1) / COO_CHUNK;
+  const int64_t chunk = coo_chunk_size(A->nnz);
+  const int64_t nchunks = (A->nnz + chunk - 1) / chunk;
   const int64_t ncarry = 2 * nchunks;
   void* scratch = nullptr;
   const size_t rows_bytes = ((sizeof(int32_t) * ncarry + 255) / 256) * 256;
@@ -189,7 +200,7 @@ int launch_coo(const mgb_coo* A, const T* x, T* y, int init, cudaStream_t s) {
   T* cv = reinterpret_cast<T*>(static_cast<char*>(scratch) + rows_bytes);
   const int64_t blocks = (nchunks + COO_WARPS - 1) / COO_WARPS;
   spmv_coo_segments<T><<<(unsigned)blocks, COO_WARPS * 32, 0, s>>>(
-      A->nrows, A->ncols, A->nnz, A->row_indices, A->column_indices,
+      A->nrows, A->ncols, A->nnz, chunk, A->row_indices, A->column_indices,
       static_cast<const T*>(A->values), x, y, init, cr, cv);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) {
@@ -280,7 +291,8 @@ int noalloc_scratch(void** out) {
 int launch_coo_noalloc_f64(const mgb_coo* A, const double* x, double* y, int init, cudaStream_t s) {
   MGB_REQUIRE(A != nullptr, MGB_ERR_BAD_ARGUMENT);
   MGB_REQUIRE(!bad_sizes(A->nrows, A->ncols, A->nnz), MGB_ERR_BAD_ARGUMENT);
-  const int64_t nchunks = (A->nnz + COO_CHUNK - 1) / COO_CHUNK;
+  const int64_t chunk = coo_chunk_size(A->nnz);
+  const int64_t nchunks = (A->nnz + chunk - 1) / chunk;
   const int64_t ncarry = 2 * nchunks;
   const size_t rows_bytes = ((sizeof(int32_t) * (size_t)ncarry + 255) / 256) * 256;
   MGB_REQUIRE(rows_bytes + sizeof(double) * (size_t)ncarry <= COO_NOALLOC_BYTES, MGB_ERR_INVALID_INPUT);
@@ -299,7 +311,7 @@ int launch_coo_noalloc_f64(const mgb_coo* A, const double* x, double* y, int ini
   double* cv = reinterpret_cast<double*>(static_cast<char*>(scratch) + rows_bytes);
   const int64_t blocks = (nchunks + COO_WARPS - 1) / COO_WARPS;
   spmv_coo_segments<double><<<(unsigned)blocks, COO_WARPS * 32, 0, s>>>(
-      A->nrows, A->ncols, A->nnz, A->row_indices, A->column_indices,
+      A->nrows, A->ncols, A->nnz, chunk, A->row_indices, A->column_indices,
       static_cast<const double*>(A->values), x, y, init, cr, cv);
   MGB_LAUNCH_CHECK();
   coo_carry_fixup<double><<<(unsigned)((ncarry + 255) / 256), 256, 0, s>>>(ncarry, A->nrows, cr, cv, y, init);

@@ -14,7 +14,8 @@
 // So the work is split by NONZEROS, not rows:
 //
 //  * Warp chunks.  Warp w takes the rows whose first entry lies in the nominal
-//    range [w*CHUNK, (w+1)*CHUNK) (two 32-ary searches over row_offsets), so
+//    range [w*CHUNK, (w+1)*CHUNK) (two 32-ary searches over row_offsets;
+//    CHUNK = 2048, smaller for matrices too small to fill the GPU), so
 //    every chunk is a whole number of rows and no row crosses warps: no
 //    atomics, no scratch, deterministic.
 //  * Lane segments.  The chunk's nonzeros [E0, E1) are cut into 32 contiguous
@@ -43,7 +44,7 @@ constexpr int CSR_WARPS = 8;  // warps per CTA
 // solver; the matrix is square there).
 template <typename T, bool DOT>
 __global__ void __launch_bounds__(CSR_WARPS * 32, 3)
-spmv_csr_segments(int64_t nrows, int64_t ncols, int64_t nnz, int64_t nchunks,
+spmv_csr_segments(int64_t nrows, int64_t ncols, int64_t nnz, int64_t nchunks, int64_t chunk,
                   const int32_t* __restrict__ ro, const int32_t* __restrict__ ci,
                   const T* __restrict__ va, const T* __restrict__ x,
                   T* __restrict__ y, int init, T* __restrict__ partials) {
@@ -53,8 +54,8 @@ spmv_csr_segments(int64_t nrows, int64_t ncols, int64_t nnz, int64_t nchunks,
   T part = T(0);
   for (int64_t wc = (int64_t)blockIdx.x * CSR_WARPS + w; wc < nchunks;
        wc += (int64_t)gridDim.x * CSR_WARPS) {
-    const csr::RowRange rr =
-        csr::csr_chunk<T, csr::CSR_CHUNK, csr::CSR_SEG>(wc, nrows, ncols, ro, ci, va, x, y, init, stage[w], lane);
+    const csr::RowRange rr = csr::csr_chunk_x<T, csr::CSR_SEG>(wc, chunk, nrows, ncols, ro, ci, va,
+                                                                 csr::XGlobal<T>{x}, y, init, stage[w], lane);
     if (DOT) {
       __syncwarp();  // the chunk's y entries, written by any lane, are visible to the warp
       for (int64_t r = rr.begin + lane; r < rr.end; r += 32) part = fmadd(x[r], y[r], part);
@@ -84,20 +85,28 @@ int launch_csr_dot(const mgb_csr* A, const T* x, T* y, int init, void* stream, i
   MGB_REQUIRE(A->row_offsets != nullptr && y != nullptr, MGB_ERR_BAD_ARGUMENT);
   MGB_REQUIRE(A->nnz == 0 || (A->column_indices && A->values && x), MGB_ERR_BAD_ARGUMENT);
   if (variant == MGB_CSR_ROWS) return launch_csr_rows<T>(A, x, y, init, as_stream(stream), partials, npartials);
-  // one extra chunk so rows whose first entry is at nnz (trailing empty rows)
-  // always belong to some chunk
-  const int64_t nchunks = A->nnz / csr::CSR_CHUNK + 1;
+  // Chunk size: 2048 nonzeros, halved (down to 256) while the matrix would
+  // give fewer chunks than the GPU holds resident warps and a chunk still
+  // spans at least 8 mean rows, so that small matrices spread over every SM
+  // (chunks hold whole rows, so splitting matrices of long rows finer only
+  // adds empty chunks).  One extra chunk so rows whose first entry is at nnz
+  // (trailing empty rows) always belong to some chunk.
+  int64_t chunk = csr::CSR_CHUNK;
+  const int64_t resident = (int64_t)num_sms() * CSR_WARPS * 3;
+  const int64_t mean_row = A->nnz / (A->nrows > 0 ? A->nrows : 1);
+  while (chunk > 256 && A->nnz / chunk < resident && chunk / 2 >= 8 * mean_row) chunk >>= 1;
+  const int64_t nchunks = A->nnz / chunk + 1;
   int64_t blocks = (nchunks + CSR_WARPS - 1) / CSR_WARPS;
   if (blocks > 0x7fffffffLL) blocks = 0x7fffffffLL;
   if (npartials) *npartials = blocks * CSR_WARPS;
   if (npartials && !partials) return MGB_SUCCESS;
   if (partials)
     spmv_csr_segments<T, true><<<(unsigned)blocks, CSR_WARPS * 32, 0, as_stream(stream)>>>(
-        A->nrows, A->ncols, A->nnz, nchunks, A->row_offsets, A->column_indices,
+        A->nrows, A->ncols, A->nnz, nchunks, chunk, A->row_offsets, A->column_indices,
         static_cast<const T*>(A->values), x, y, init, partials);
   else
     spmv_csr_segments<T, false><<<(unsigned)blocks, CSR_WARPS * 32, 0, as_stream(stream)>>>(
-        A->nrows, A->ncols, A->nnz, nchunks, A->row_offsets, A->column_indices,
+        A->nrows, A->ncols, A->nnz, nchunks, chunk, A->row_offsets, A->column_indices,
         static_cast<const T*>(A->values), x, y, init, nullptr);
   MGB_LAUNCH_CHECK();
   return MGB_SUCCESS;

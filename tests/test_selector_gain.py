@@ -10,10 +10,13 @@ is the network trained on the training part.  Both were written by one run of
         --corpus-out tests/golden/selector_corpus.npz
 
 On the held-out matrices the learned choice must stay within 10 % of the
-exhaustive best time on average (mean regret), be >= 1.5x faster than CSR
-only (geometric mean), and beat the rule-based selector whose thresholds are
-tuned on the same training matrices.  The CPU test runs the network through
-the FP64 oracle; the GPU test through the library's forward kernel.
+exhaustive best time on average (mean regret), capture at least 90 % of the
+exhaustive oracle's (log) speed-up over CSR only, and beat the rule-based
+selector whose thresholds are tuned on the same training matrices.  (The
+absolute speed-up over CSR only is bounded by the oracle's: with the
+adaptive-chunk CSR kernel the best format is 1.42x faster than CSR on this
+corpus in geometric mean.)  The CPU test runs the network through the FP64
+oracle; the GPU test through the library's forward kernel.
 """
 import os
 
@@ -44,7 +47,9 @@ def _check_gain(choice, c):
     thr = selector.tune_rule(c["Xtr"], c["Ftr"], c["Ttr"])
     rule = selector.evaluate(c["Tte"], selector.rule_select(c["Xte"], c["Fte"], **thr))
     assert learned["mean_regret"] <= 0.10, learned
-    assert learned["geomean_speedup_vs_csr"] >= 1.5, learned
+    oracle = learned["oracle_geomean_speedup_vs_csr"]
+    assert np.log(learned["geomean_speedup_vs_csr"]) >= 0.9 * np.log(oracle), learned
+    assert learned["geomean_speedup_vs_csr"] >= 1.3, learned
     assert learned["mean_regret"] < rule["mean_regret"], (learned, rule)
     assert learned["geomean_speedup_vs_csr"] > rule["geomean_speedup_vs_csr"], (learned, rule)
     return learned, rule
