@@ -373,15 +373,29 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
                 used.add(i)
                 break
     e2e_steps = max(1, min(args.steps, args.e2e_steps))
+    e2e_api = "torch copies + multiply"
+    host_csr = None
+    if args.format == "csr":
+        # the library's host-data entry point: pipelined block copies + kernels
+        host_csr = mgb.matrix_from_host(hm, device="cpu", dtype=tdtype)
+        host_csr._ro = pinned[id(hm["row_offsets"])]
+        host_csr._ci = pinned[id(hm["column_indices"])]
+        host_csr._v = pinned[id(hm["values"])].to(tdtype) if pinned[id(hm["values"])].dtype != tdtype \
+            else pinned[id(hm["values"])]
+        e2e_api = "multiply_host (mgb_spmv_csr_host, pipelined row blocks)"
+        mgb.multiply_host(host_csr, xh, yh, init=True)  # warm-up (pool allocation, kernel choice)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for _ in range(e2e_steps):
-        for h, d in pairs:
-            d.copy_(h, non_blocking=True)
-        x.copy_(xh, non_blocking=True)
-        mgb.multiply(dev_bufs, x, y, init=True)
-        yh.copy_(y, non_blocking=True)
+        if host_csr is not None:
+            mgb.multiply_host(host_csr, xh, yh, init=True)
+        else:
+            for h, d in pairs:
+                d.copy_(h, non_blocking=True)
+            x.copy_(xh, non_blocking=True)
+            mgb.multiply(dev_bufs, x, y, init=True)
+            yh.copy_(y, non_blocking=True)
     e1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = e0.elapsed_time(e1) / e2e_steps
@@ -405,7 +419,7 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
                      "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured"
                      else "fallback 6.8 TB/s", "algorithmic_bytes_per_launch": nbytes},
         "e2e": {"value": e2e_val, "unit": "GB/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "ms_per_step": e2e_ms},
+                "ms_per_step": e2e_ms, "api": e2e_api},
         "gpu_launches": args.steps * launches_per_step(hm),
         "clocks": clocks,
     }

@@ -348,6 +348,23 @@ int mgb_coo_sort_by_row_and_column_f32(mgb_coo* A, void* stream);
 /* impl/Coo/Serial/Morpheus_Sort_Impl.hpp:166-186; *sorted = 1 or 0 */
 int mgb_coo_is_sorted(const mgb_coo* A, int* sorted, void* stream);
 
+/* ---- CSR SpMV from host memory --------------------------------------------
+ * y = A*x (init) or y += A*x where the descriptor's arrays, x and y are HOST
+ * pointers (pinned memory for overlap): the matrix is copied in nblocks
+ * nnz-balanced row blocks (nblocks <= 0: 2; at most 64) and
+ * block b is multiplied while block b+1 is in flight, y coming back per block.
+ * The host-space counterpart of the reference's Serial / OpenMP multiply on
+ * host containers (impl/Csr/Serial/Morpheus_Multiply_Impl.hpp:38-58).
+ * `variant` as for mgb_spmv_csr_variant_*; `workspace` a device buffer of
+ * mgb_spmv_csr_host_workspace_bytes (or NULL).  Synchronises the stream. */
+int mgb_spmv_csr_host_f64(const mgb_csr* A, const double* x, double* y, int init, int variant, int64_t nblocks,
+                          void* workspace, int64_t workspace_bytes, void* stream);
+int mgb_spmv_csr_host_f32(const mgb_csr* A, const float* x, float* y, int init, int variant, int64_t nblocks,
+                          void* workspace, int64_t workspace_bytes, void* stream);
+/* Device workspace for the host-data SpMV (256-byte aligned; NULL workspace:
+ * the call takes stream-ordered scratch instead).  value_bytes 8 or 4. */
+int mgb_spmv_csr_host_workspace_bytes(const mgb_csr* A, int value_bytes, int64_t* bytes);
+
 /* ---- fused solver steps (no reference counterpart) -----------------------
  * The steps either side of SpMV in an iterative solver, fused into the pass
  * that produces their input; a CG written on the reference's multiply / dot /

@@ -4,7 +4,7 @@ Host-side mirror of the reference's container/algorithm API over the C ABI of
 libmorpheus_gb300.so (sm_103a kernels).  See include/mgb.h for the ABI and
 include/Morpheus_GB300.hpp for the C++ front end.
 """
-from .algorithms import dot, dot_async, multiply, reduce, waxpby
+from .algorithms import dot, dot_async, multiply, multiply_host, reduce, waxpby
 from .batched import CsrBatch
 from .convert import convert, convert_inplace, from_coo, is_sorted, sort_by_row_and_column, to_coo
 from .containers import (COO_FORMAT, CSR_FORMAT, DIA_FORMAT, ELL_FORMAT, HDC_FORMAT, HYB_FORMAT,
@@ -18,7 +18,7 @@ from .exceptions import (AllocationException, BadArgumentException, CudaExceptio
                          TimeoutException)
 
 __all__ = [
-    "multiply", "dot", "dot_async", "reduce", "waxpby",
+    "multiply", "multiply_host", "dot", "dot_async", "reduce", "waxpby",
     "convert", "convert_inplace", "to_coo", "from_coo", "sort_by_row_and_column", "is_sorted",
     "CooMatrix", "CsrMatrix", "DiaMatrix", "EllMatrix", "HybMatrix", "HdcMatrix", "DynamicMatrix",
     "formats_e", "conversion_error_e", "get_pad_size", "matrix_from_host", "matrix_to_host",

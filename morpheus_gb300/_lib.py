@@ -99,6 +99,9 @@ for _dt, _ct in (("f64", C.c_double), ("f32", C.c_float)):
     _SIGS[f"mgb_waxpby_dot_{_dt}"] = (C.c_int, [i64, _ct, vp, _ct, vp, vp, vp, vp])
     _SIGS[f"mgb_cg_csr_{_dt}"] = (C.c_int, [C.POINTER(Csr), C.c_int, vp, vp, i64, C.c_double, C.POINTER(i64),
                                             C.POINTER(C.c_double), vp])
+for _dt in ("f64", "f32"):
+    _SIGS[f"mgb_spmv_csr_host_{_dt}"] = (C.c_int, [C.POINTER(Csr), vp, vp, C.c_int, C.c_int, i64, vp, i64, vp])
+_SIGS["mgb_spmv_csr_host_workspace_bytes"] = (C.c_int, [C.POINTER(Csr), C.c_int, C.POINTER(i64)])
 _SIGS["mgb_spmv_coo_f64_noalloc"] = (C.c_int, [C.POINTER(Coo), vp, vp, C.c_int, vp])
 _P = C.POINTER
 for _name, _s, _d in (("csr_to_coo", Csr, Coo), ("coo_to_csr", Coo, Csr), ("dia_to_coo", Dia, Coo),

@@ -18,8 +18,8 @@ import ctypes as C
 import torch
 
 from . import _lib
-from .containers import (COO_FORMAT, CSR_FORMAT, DIA_FORMAT, ELL_FORMAT, HDC_FORMAT, HYB_FORMAT,
-                         DynamicMatrix, _Matrix)
+from .containers import (COO_FORMAT, CSR_FORMAT, CSR_ROWS, CSR_SEGMENTS, DIA_FORMAT, ELL_FORMAT, HDC_FORMAT,
+                         HYB_FORMAT, DynamicMatrix, _Matrix)
 from .exceptions import InvalidInputException, NotImplementedException
 
 _FMT_NAME = {COO_FORMAT: "coo", CSR_FORMAT: "csr", DIA_FORMAT: "dia", ELL_FORMAT: "ell",
@@ -77,6 +77,53 @@ def multiply(A: _Matrix, x, y, init: bool = True, stream=None) -> None:
     name = f"mgb_spmv_{_FMT_NAME[A.FORMAT]}_{_suffix(A.dtype)}"
     _lib.call(name, C.byref(desc), C.c_void_p(xt.data_ptr()), C.c_void_p(yt.data_ptr()),
               1 if init else 0, _stream_handle(stream))
+
+
+def host_kernel_variant(A) -> int:
+    """CSR kernel choice for a host-resident CsrMatrix, by the rule of
+    mgb_csr_choose_kernel (row-tile kernel when the longest row is <= 28 and
+    <= 1.5 x mean + 2), computed once on the host and cached."""
+    v = getattr(A, "_variant", None)
+    if v is None:
+        lens = (A.row_offsets()[1:] - A.row_offsets()[:-1]) if A.nrows() else None
+        if lens is None or A.nnnz() == 0:
+            v = CSR_SEGMENTS
+        else:
+            mx = int(lens.max().item())
+            mean = A.nnnz() / A.nrows()
+            v = CSR_ROWS if (32 * mx <= 896 and mx <= 1.5 * mean + 2.0) else CSR_SEGMENTS
+        A._variant = v
+    return v
+
+
+def multiply_host(A, x, y, init: bool = True, nblocks: int = 0, stream=None) -> None:
+    """y = A*x (or y += A*x) for a CsrMatrix, x and y in HOST memory (pin them
+    for overlap): the matrix goes to the GPU in row blocks that are
+    multiplied while the next block is copied.  Synchronous."""
+    if isinstance(A, DynamicMatrix):
+        A = A.active()
+    if A.FORMAT != CSR_FORMAT:
+        raise NotImplementedException("multiply_host takes a CsrMatrix")
+    if A.device.type != "cpu":
+        raise InvalidInputException("multiply_host takes a host-resident matrix (use multiply for device data)")
+    for t in (x, y):
+        if not isinstance(t, torch.Tensor) or t.device.type != "cpu" or not t.is_contiguous():
+            raise InvalidInputException("x and y must be contiguous host tensors")
+    if x.dtype != A.dtype or y.dtype != A.dtype:
+        raise InvalidInputException("x, y and A must share the value type")
+    if x.numel() < A.ncols() or y.numel() < A.nrows():
+        raise InvalidInputException("x or y too short for A")
+    desc = A._desc()
+    # the device workspace is kept with the matrix (no allocation per call)
+    dev = torch.cuda.current_device()
+    ws = getattr(A, "_host_ws", None)
+    if ws is None or ws.device.index != dev:
+        nb = C.c_int64()
+        _lib.call("mgb_spmv_csr_host_workspace_bytes", C.byref(desc), A.dtype.itemsize, C.byref(nb))
+        ws = A._host_ws = torch.empty(max(nb.value, 1), dtype=torch.uint8, device=f"cuda:{dev}")
+    _lib.call(f"mgb_spmv_csr_host_{_suffix(A.dtype)}", C.byref(desc), C.c_void_p(x.data_ptr()),
+              C.c_void_p(y.data_ptr()), 1 if init else 0, host_kernel_variant(A), int(nblocks),
+              C.c_void_p(ws.data_ptr()), ws.numel(), _stream_handle(stream))
 
 
 def dot(n: int, x, y, stream=None) -> float:
