@@ -18,7 +18,7 @@ import ctypes as C
 import torch
 
 from . import _lib
-from .containers import (COO_FORMAT, CSR_FORMAT, CSR_ROWS, CSR_SEGMENTS, DIA_FORMAT, ELL_FORMAT, HDC_FORMAT,
+from .containers import (COO_FORMAT, CSR_FORMAT, CSR_ROWS, CSR_SEGMENTS, CSR_SPLIT, DIA_FORMAT, ELL_FORMAT, HDC_FORMAT,
                          HYB_FORMAT, DynamicMatrix, _Matrix)
 from .exceptions import InvalidInputException, NotImplementedException
 
@@ -82,7 +82,9 @@ def multiply(A: _Matrix, x, y, init: bool = True, stream=None) -> None:
 def host_kernel_variant(A) -> int:
     """CSR kernel choice for a host-resident CsrMatrix, by the rule of
     mgb_csr_choose_kernel (row-tile kernel when the longest row is <= 28 and
-    <= 1.5 x mean + 2), computed once on the host and cached."""
+    <= 1.5 x mean + 2; split kernel when a row is longer than 8192 or rows
+    average >= 512),
+    computed once on the host and cached."""
     v = getattr(A, "_variant", None)
     if v is None:
         lens = (A.row_offsets()[1:] - A.row_offsets()[:-1]) if A.nrows() else None
@@ -92,6 +94,8 @@ def host_kernel_variant(A) -> int:
             mx = int(lens.max().item())
             mean = A.nnnz() / A.nrows()
             v = CSR_ROWS if (32 * mx <= 896 and mx <= 1.5 * mean + 2.0) else CSR_SEGMENTS
+            if mx > 8192 or mean >= 512:
+                v = CSR_SPLIT
         A._variant = v
     return v
 

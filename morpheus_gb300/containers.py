@@ -44,8 +44,8 @@ class conversion_error_e(enum.IntEnum):
 
 COO_FORMAT, CSR_FORMAT, DIA_FORMAT, ELL_FORMAT, HYB_FORMAT, HDC_FORMAT, NFORMATS = range(7)
 INVALID_INDEX = -1
-# CSR SpMV kernels (MGB_CSR_SEGMENTS / MGB_CSR_ROWS of include/mgb.h)
-CSR_SEGMENTS, CSR_ROWS = 1, 2
+# CSR SpMV kernels (MGB_CSR_SEGMENTS / MGB_CSR_ROWS / MGB_CSR_SPLIT of include/mgb.h)
+CSR_SEGMENTS, CSR_ROWS, CSR_SPLIT = 1, 2, 3
 
 
 def get_pad_size(length: int, alignment: int) -> int:

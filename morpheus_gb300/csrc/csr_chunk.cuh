@@ -201,3 +201,168 @@ __device__ __forceinline__ RowRange csr_chunk(int64_t wc, int64_t nrows, int64_t
 
 }  // namespace csr
 }  // namespace mgb
+
+namespace mgb {
+namespace csr {
+
+// Split chunk k of a CSR matrix: exactly the entries [k*chunk, min((k+1)*chunk,
+// nnz)), whatever rows they belong to (rows longer than a chunk are spread
+// over several warps).  Rows that start and end inside the chunk are written
+// to y; the row continuing from the previous chunk (started before E0) and
+// the row continuing into the next one (ends after E1) leave their partial
+// sums as carries: carry slot 2k for the row entering the chunk, 2k+1 for
+// the row leaving it, (-1, 0) when there is none (a row spanning the whole
+// chunk fills both slots, so each row's carries stay consecutive).  A carry
+// fix-up adds them in chunk order.  Empty rows are zero-filled (init) by the
+// chunk whose range holds their start offset; trailing empty rows (start ==
+// nnz) by the last chunk's last lane.
+template <typename T, int SEG>
+__device__ __forceinline__ void csr_split_chunk(int64_t k, int64_t chunk, int64_t nchunks, int64_t nrows,
+                                                int64_t ncols, int64_t nnz, const int32_t* __restrict__ ro,
+                                                const int32_t* __restrict__ ci, const T* __restrict__ va,
+                                                const T* __restrict__ x, T* __restrict__ y, int init,
+                                                int32_t* __restrict__ carry_row, T* __restrict__ carry_val,
+                                                WarpStage<T, SEG>& stg, int lane) {
+  constexpr int CSR_PAD = SEG + 1;
+  T* sv = stg.val;
+  int32_t* sc = stg.col;
+  int32_t* sro = stg.ro;
+  const int64_t E0 = k * chunk;
+  const int64_t E1 = min(E0 + chunk, nnz);
+  const bool last = k == nchunks - 1;
+  // rows starting in [E0, E1) (all remaining rows for the last chunk)
+  const int64_t r_a = warp_lower_bound(ro, 0, nrows + 1, E0, lane);
+  const int64_t r_end = last ? nrows : min(warp_lower_bound(ro, r_a, nrows + 1, E1, lane), nrows);
+  // the row entering the chunk: started before E0, still has entries at E0
+  const bool has_in = E0 < E1 && r_a > 0 && (r_a > nrows || (int64_t)__ldg(ro + r_a) > E0);
+  const int64_t r_lo = has_in ? r_a - 1 : r_a;  // first row the lanes walk
+  const int64_t r_hi = r_end;                   // rows [r_lo, r_hi)
+  if (lane == 0) {
+    carry_row[2 * k] = -1;
+    carry_val[2 * k] = T(0);
+    carry_row[2 * k + 1] = -1;
+    carry_val[2 * k + 1] = T(0);
+  }
+  if (r_lo >= r_hi) return;
+  const int64_t nr = r_hi - r_lo;
+  const bool staged = nr < CSR_RO_STAGE;
+  __syncwarp();
+  if (staged)
+    for (int64_t i = lane; i <= nr; i += 32) sro[i] = __ldg(ro + r_lo + i);
+  __syncwarp();
+  auto ro_at = [&](int64_t i) -> int64_t { return staged ? (int64_t)sro[i - r_lo] : (int64_t)__ldg(ro + i); };
+  // the row leaving the chunk: ends after E1 (only the last row can)
+  const int64_t r_out = (r_hi > r_lo && ro_at(r_hi) > E1) ? r_hi - 1 : -1;
+  auto put = [&](int64_t r, T v) {  // a finished sum of row r over this chunk
+    if (has_in && r == r_lo) {
+      carry_row[2 * k] = (int32_t)r;
+      carry_val[2 * k] = v;
+      if (r == r_out) carry_row[2 * k + 1] = (int32_t)r;  // spans the chunk: keep its carries consecutive
+    } else if (r == r_out) {
+      carry_row[2 * k + 1] = (int32_t)r;
+      carry_val[2 * k + 1] = v;
+    } else {
+      y[r] = v;
+    }
+  };
+  if (E0 >= E1) {  // no entries (nnz == 0 handled by the launcher; only empty rows here)
+    if (init)
+      for (int64_t r = r_lo + lane; r < r_hi; r += 32) y[r] = T(0);
+    return;
+  }
+  const int64_t A0 = E0 & ~(int64_t)7;
+  int64_t KW = (E1 - A0 + 31) / 32;
+  KW = (KW + SEG - 1) / SEG * SEG;
+  const int64_t la = A0 + lane * KW;
+  const int64_t lb = min(la + KW, E1);
+  const int64_t e_lo = max(la, E0);
+  const bool active = e_lo < lb;
+  int64_t r = r_hi;
+  if (active) {
+    if (lane == 0) {
+      r = r_lo;
+    } else {
+      int64_t lo = r_lo, hi = r_hi;  // first i in [lo, hi] with ro[i] > e_lo
+      while (lo < hi) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (ro_at(mid) <= e_lo) lo = mid + 1; else hi = mid;
+      }
+      r = lo - 1;
+    }
+  }
+  int64_t rs = active ? ro_at(r) : 0;
+  int64_t re = active ? ro_at(r + 1) : 0;
+  // seed with y only rows that start in this lane and end in this chunk
+  auto seed = [&](int64_t rr, int64_t s, int64_t e) -> T {
+    return (!init && s >= e_lo && e <= E1 && !(has_in && rr == r_lo)) ? y[rr] : T(0);
+  };
+  T acc = active ? seed(r, rs, re) : T(0);
+  int64_t hrow = -1;
+  T hval = T(0);
+  for (int64_t s = 0; s < KW; s += SEG) {
+    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < SEG; q++) {
+      const int f = q * 32 + lane;
+      const int L = f / SEG, j = f % SEG;
+      const int64_t e = A0 + L * KW + s + j;
+      const bool in = e >= E0 && e < E1;
+      sv[L * CSR_PAD + j] = in ? ldg_stream(va + e) : T(0);
+      sc[L * CSR_PAD + j] = in ? ldg_stream(ci + e) : 0;
+    }
+    __syncwarp();
+    T v[SEG], xv[SEG];
+#pragma unroll
+    for (int q = 0; q < SEG; q++) {
+      const int64_t e = la + s + q;
+      const bool valid = e >= e_lo && e < lb;
+      const int32_t c = sc[lane * CSR_PAD + q];
+      v[q] = valid ? sv[lane * CSR_PAD + q] : T(0);
+      xv[q] = (valid && (uint64_t)(int64_t)c < (uint64_t)ncols) ? __ldg(x + c) : T(0);
+    }
+#pragma unroll
+    for (int q = 0; q < SEG; q++) {
+      const int64_t e = la + s + q;
+      const bool valid = e >= e_lo && e < lb;
+      while (valid && e >= re) {
+        if (rs >= e_lo) { put(r, acc); } else { hrow = r; hval = acc; }
+        r++;
+        rs = re;
+        re = ro_at(r + 1);
+        acc = seed(r, rs, re);
+      }
+      acc = fmadd(v[q], xv[q], acc);
+    }
+  }
+  // rows ending exactly at the lane end (and empty rows sitting there)
+  if (active) {
+    while (r < r_hi && re <= lb) {
+      if (rs >= e_lo) { put(r, acc); } else { hrow = r; hval = acc; }
+      r++;
+      if (r < r_hi) {
+        rs = re;
+        re = ro_at(r + 1);
+        acc = seed(r, rs, re);
+      }
+    }
+  }
+  // tail partials and the segmented scan, as in csr_chunk_x; the row leaving
+  // the chunk ends in no lane: the last lane holding it writes its carry
+  const bool has_tail = active && r < r_hi && rs < lb;
+  const int64_t key = has_tail ? r : -1 - (int64_t)lane;
+  T cv = has_tail ? acc : T(0);
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const T u = __shfl_up_sync(0xffffffffu, cv, d);
+    const int64_t k2 = __shfl_up_sync(0xffffffffu, key, d);
+    if (lane >= d && k2 == key) cv += u;
+  }
+  const T vprev = __shfl_up_sync(0xffffffffu, cv, 1);
+  const int64_t kprev = __shfl_up_sync(0xffffffffu, key, 1);
+  const int64_t knext = __shfl_down_sync(0xffffffffu, key, 1);
+  if (hrow >= 0) put(hrow, (lane > 0 && kprev == hrow) ? hval + vprev : hval);
+  if (has_tail && r == r_out && (lane == 31 || knext != key)) put(r, cv);
+}
+
+}  // namespace csr
+}  // namespace mgb

@@ -67,6 +67,93 @@ spmv_csr_segments(int64_t nrows, int64_t ncols, int64_t nnz, int64_t nchunks, in
   }
 }
 
+// Split variant: fixed nonzero chunks (rows of any length spread over
+// warps), carries for the rows crossing chunk ends, fixed-order fix-up.
+template <typename T>
+__global__ void __launch_bounds__(CSR_WARPS * 32, 3)
+spmv_csr_split(int64_t nrows, int64_t ncols, int64_t nnz, int64_t nchunks, int64_t chunk,
+               const int32_t* __restrict__ ro, const int32_t* __restrict__ ci, const T* __restrict__ va,
+               const T* __restrict__ x, T* __restrict__ y, int init, int32_t* __restrict__ carry_row,
+               T* __restrict__ carry_val) {
+  __shared__ csr::WarpStage<T, csr::CSR_SEG> stage[CSR_WARPS];
+  const int lane = threadIdx.x & 31;
+  const int w = threadIdx.x >> 5;
+  for (int64_t k = (int64_t)blockIdx.x * CSR_WARPS + w; k < nchunks; k += (int64_t)gridDim.x * CSR_WARPS)
+    csr::csr_split_chunk<T, csr::CSR_SEG>(k, chunk, nchunks, nrows, ncols, nnz, ro, ci, va, x, y, init, carry_row,
+                                          carry_val, stage[w], lane);
+}
+
+// y[r] = (init ? 0 : y[r]) + the carries of row r, added in chunk order; a
+// row's carries are consecutive (rows < 0 mark empty slots)
+template <typename T>
+__global__ void split_carry_fixup(int64_t ncarry, int64_t nrows, const int32_t* __restrict__ cr,
+                                  const T* __restrict__ cv, T* __restrict__ y, int init) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ncarry) return;
+  const int32_t r = cr[i];
+  if (r < 0 || r >= nrows || (i > 0 && cr[i - 1] == r)) return;
+  T s = init ? T(0) : y[r];
+  for (int64_t j = i; j < ncarry && cr[j] == r; j++) s += cv[j];
+  y[r] = s;
+}
+
+// x[0..n) . y[0..n) into per-block partials (the split variant's fused dot,
+// after its fix-up)
+template <typename T>
+__global__ void __launch_bounds__(256) rows_dot_partials(const T* __restrict__ x, const T* __restrict__ y, int64_t n,
+                                                         T* __restrict__ partials) {
+  __shared__ T s[8];
+  T a = T(0);
+  for (int64_t i = (int64_t)blockIdx.x * 256 + threadIdx.x; i < n; i += (int64_t)gridDim.x * 256)
+    a = fmadd(x[i], y[i], a);
+  a = warp_sum(a);
+  if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = a;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    T t = threadIdx.x < 8 ? s[threadIdx.x] : T(0);
+    t = warp_sum(t);
+    if (threadIdx.x == 0) partials[blockIdx.x] = t;
+  }
+}
+
+template <typename T>
+int launch_split(const mgb_csr* A, const T* x, T* y, int init, cudaStream_t s, T* partials, int64_t* npartials) {
+  const int64_t dot_blocks = (int64_t)num_sms() * 4;
+  if (npartials) *npartials = dot_blocks;
+  if (npartials && !partials) return MGB_SUCCESS;
+  if (A->nnz == 0) {
+    if (init) MGB_CUDA_CHECK(cudaMemsetAsync(y, 0, sizeof(T) * A->nrows, s));
+  } else {
+    const int64_t chunk = csr::CSR_CHUNK;
+    const int64_t nchunks = (A->nnz + chunk - 1) / chunk;
+    const int64_t ncarry = 2 * nchunks;
+    void* scratch = nullptr;
+    const size_t rows_bytes = ((sizeof(int32_t) * (size_t)ncarry + 255) / 256) * 256;
+    MGB_CUDA_CHECK(cudaMallocAsync(&scratch, rows_bytes + sizeof(T) * (size_t)ncarry, s));
+    int32_t* cr = static_cast<int32_t*>(scratch);
+    T* cv = reinterpret_cast<T*>(static_cast<char*>(scratch) + rows_bytes);
+    int64_t blocks = (nchunks + CSR_WARPS - 1) / CSR_WARPS;
+    if (blocks > 0x7fffffffLL) blocks = 0x7fffffffLL;
+    spmv_csr_split<T><<<(unsigned)blocks, CSR_WARPS * 32, 0, s>>>(A->nrows, A->ncols, A->nnz, nchunks, chunk,
+                                                                  A->row_offsets, A->column_indices,
+                                                                  static_cast<const T*>(A->values), x, y, init, cr,
+                                                                  cv);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) {
+      split_carry_fixup<T><<<(unsigned)((ncarry + 255) / 256), 256, 0, s>>>(ncarry, A->nrows, cr, cv, y, init);
+      e = cudaGetLastError();
+    }
+    const cudaError_t ef = cudaFreeAsync(scratch, s);
+    if (e != cudaSuccess) return record_cuda_error(e);
+    if (ef != cudaSuccess) return record_cuda_error(ef);
+  }
+  if (partials) {
+    rows_dot_partials<T><<<(unsigned)dot_blocks, 256, 0, s>>>(x, y, A->nrows, partials);
+    MGB_LAUNCH_CHECK();
+  }
+  return MGB_SUCCESS;
+}
+
 template <typename T>
 int launch_csr(const mgb_csr* A, const T* x, T* y, int init, void* stream, int variant = MGB_CSR_SEGMENTS) {
   return launch_csr_dot<T>(A, x, y, init, stream, variant, nullptr, nullptr);
@@ -80,11 +167,13 @@ int launch_csr_dot(const mgb_csr* A, const T* x, T* y, int init, void* stream, i
   MGB_REQUIRE(A != nullptr, MGB_ERR_BAD_ARGUMENT);
   MGB_REQUIRE(!bad_sizes(A->nrows, A->ncols, A->nnz), MGB_ERR_BAD_ARGUMENT);
   MGB_REQUIRE(A->nnz < ((int64_t)1 << 31) - 4096, MGB_ERR_INVALID_INPUT);
-  MGB_REQUIRE(variant == MGB_CSR_SEGMENTS || variant == MGB_CSR_ROWS, MGB_ERR_BAD_ARGUMENT);
+  MGB_REQUIRE(variant == MGB_CSR_SEGMENTS || variant == MGB_CSR_ROWS || variant == MGB_CSR_SPLIT,
+              MGB_ERR_BAD_ARGUMENT);
   if (A->nrows == 0) return MGB_SUCCESS;
   MGB_REQUIRE(A->row_offsets != nullptr && y != nullptr, MGB_ERR_BAD_ARGUMENT);
   MGB_REQUIRE(A->nnz == 0 || (A->column_indices && A->values && x), MGB_ERR_BAD_ARGUMENT);
   if (variant == MGB_CSR_ROWS) return launch_csr_rows<T>(A, x, y, init, as_stream(stream), partials, npartials);
+  if (variant == MGB_CSR_SPLIT) return launch_split<T>(A, x, y, init, as_stream(stream), partials, npartials);
   // Chunk size: 2048 nonzeros, halved (down to 256) while the matrix would
   // give fewer chunks than the GPU holds resident warps and a chunk still
   // spans at least 8 mean rows, so that small matrices spread over every SM

@@ -8,6 +8,9 @@
 //   MGB_CSR_ROWS     when 32 rows of the longest length fit one staged tile
 //                    (longest row <= 28) and the longest row is <= 1.5 x
 //                    mean + 2 (stencils, banded matrices, FEM meshes), else
+//   MGB_CSR_SPLIT    when some row is longer than 8192 entries or rows
+//                    average >= 512 (split nonzero chunks with carries,
+//                    spmv_csr.cu), else
 //   MGB_CSR_SEGMENTS the lane-segment kernel of spmv_csr.cu (any structure).
 //
 // Row-tile kernel: one warp owns 32 consecutive rows.  The tile's entries are
@@ -131,6 +134,10 @@ int choose(const mgb_csr* A, int* variant, cudaStream_t s) {
   if (e != cudaSuccess) return record_cuda_error(e);
   const double mean = (double)A->nnz / (double)A->nrows;
   if (32 * mx <= ROWS_TILE_MAX && (double)mx <= 1.5 * mean + 2.0) *variant = MGB_CSR_ROWS;
+  // rows longer than a few chunks: one warp per row would be the critical
+  // path (measured: a 150,000-entry row 746 -> 56 us; rows of 1,000-6,000
+  // entries 66 -> 46 us; the power-law matrix, mean 15, stays faster whole)
+  if (mx > 8192 || mean >= 512.0) *variant = MGB_CSR_SPLIT;
   return MGB_SUCCESS;
 }
 

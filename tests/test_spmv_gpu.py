@@ -184,12 +184,21 @@ def _csr_case(case, dtype):
         return gen.random_lengths_csr(100, 50000, lens, seed=25, dtype=dtype)
     if case == "ragged_tail":  # nrows not a multiple of 32
         return gen.random_lengths_csr(1000 * 32 + 7, 5000, np.full(32007, 9), seed=26, dtype=dtype)
+    if case == "huge_row":  # one row spanning many 2048-entry chunks, empty rows around it
+        lens = np.where(np.arange(4000) % 3 == 0, 2, 0)
+        lens[1500] = 150000
+        lens[1501] = 2047
+        return gen.random_lengths_csr(4000, 200000, lens, seed=27, dtype=dtype)
+    if case == "all_empty_tail":  # entries only in the first rows, long empty tail
+        lens = np.zeros(10000, dtype=np.int64)
+        lens[:50] = 4096
+        return gen.random_lengths_csr(10000, 9000, lens, seed=28, dtype=dtype)
     raise ValueError(case)
 
 
-@pytest.mark.parametrize("variant", [mgb.CSR_SEGMENTS, mgb.CSR_ROWS])
+@pytest.mark.parametrize("variant", [mgb.CSR_SEGMENTS, mgb.CSR_ROWS, mgb.CSR_SPLIT])
 @pytest.mark.parametrize("case", ["stencil27", "laplacian", "banded", "power_law", "empty_rows",
-                                  "long_rows", "ragged_tail"])
+                                  "long_rows", "ragged_tail", "huge_row", "all_empty_tail"])
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
 def test_csr_kernel_variants(cuda, variant, case, dtype):
     """Both CSR kernels give the Serial result on every structure, whichever
@@ -200,11 +209,11 @@ def test_csr_kernel_variants(cuda, variant, case, dtype):
 
 
 @pytest.mark.parametrize("case,expect", [("stencil27", "rows"), ("laplacian", "rows"), ("banded", "rows"),
-                                         ("power_law", "segments"), ("long_rows", "segments"),
-                                         ("empty_rows", "segments")])
+                                         ("power_law", "segments"), ("long_rows", "split"),
+                                         ("empty_rows", "segments"), ("huge_row", "split")])
 def test_csr_kernel_choice(cuda, case, expect):
     A = mgb.matrix_from_host(_csr_case(case, np.float64), device="cuda")
-    want = mgb.CSR_ROWS if expect == "rows" else mgb.CSR_SEGMENTS
+    want = {"rows": mgb.CSR_ROWS, "segments": mgb.CSR_SEGMENTS, "split": mgb.CSR_SPLIT}[expect]
     assert A.kernel_variant() == want
 
 
