@@ -420,6 +420,7 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
                      else "fallback 6.8 TB/s", "algorithmic_bytes_per_launch": nbytes},
         "e2e": {"value": e2e_val, "unit": "GB/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": e2e_ms, "api": e2e_api},
+        "gflops": 2.0 * hm["nnz"] / (kernel_ms * 1e-3) / 1e9 if hm.get("nnz") else None,
         "gpu_launches": args.steps * launches_per_step(hm),
         "clocks": clocks,
     }
@@ -429,9 +430,13 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
         threads = O.max_threads()
         times = cpu_multiply_timing(hm, x_np, args.cpu_budget, threads)
         med = statistics.median(times)
+        # the Serial algorithm on one core, a bounded sample (about 3 s)
+        st = cpu_multiply_timing(hm, x_np, min(3.0, args.cpu_budget), 0, min_reps=1)
         line["cpu_baseline"] = {"value": nbytes / med / 1e9, "unit": "GB/s", "cores": threads, "kind": "port",
                                 "sample": f"full matrix, {len(times)} multiplies over ~{args.cpu_budget:.0f} s, "
-                                          "median (reference OpenMP algorithm restated in oracle/oracle.cpp)"}
+                                          "median (reference OpenMP algorithm restated in oracle/oracle.cpp)",
+                                "serial_1_core": {"value": nbytes / statistics.median(st) / 1e9, "unit": "GB/s",
+                                                  "sample": f"{len(st)} Serial multiplies, median"}}
     print(json.dumps(line), flush=True)
 
 

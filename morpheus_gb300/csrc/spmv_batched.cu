@@ -31,13 +31,14 @@ namespace mgb {
 namespace {
 
 constexpr int BAT_WARPS = 8;
-constexpr int BAT_NCONFIGS = 8;
-constexpr int BAT_FIRST_XS = 6;  // configurations >= this keep x in shared memory
+constexpr int BAT_NCONFIGS = 10;
+constexpr int BAT_FIRST_XS = 6;  // configurations 6, 7 keep x in shared memory
+constexpr int BAT_FIRST_XL1 = 8;  // configurations 8, 9: matrix per CTA, x through L1
 // chunk-queue configs: nonzeros per chunk; matrix-per-CTA configs: 0 (each
 // matrix is cut into 8 x BAT_XS_CPW chunks of at least 256 nonzeros)
-constexpr int64_t BAT_CHUNK[BAT_NCONFIGS] = {512, 1024, 2048, 4096, 1024, 2048, 0, 0};
-constexpr int BAT_SEG[BAT_NCONFIGS] = {8, 8, 8, 8, 4, 4, 8, 8};
-constexpr int BAT_XS_CPW[BAT_NCONFIGS] = {0, 0, 0, 0, 0, 0, 1, 2};  // chunks per warp
+constexpr int64_t BAT_CHUNK[BAT_NCONFIGS] = {512, 1024, 2048, 4096, 1024, 2048, 0, 0, 0, 0};
+constexpr int BAT_SEG[BAT_NCONFIGS] = {8, 8, 8, 8, 4, 4, 8, 8, 8, 8};
+constexpr int BAT_XS_CPW[BAT_NCONFIGS] = {0, 0, 0, 0, 0, 0, 1, 2, 1, 2};  // chunks per warp
 constexpr int BAT_XS_BYTES = 32 * 1024;  // per x buffer, two buffers (larger x: read from global)
 // workspace: int32 header[4] = {work counter, total work items, planned
 // config, error flag}, then int32[nitems + 1]: the chunk prefix (chunk-queue
@@ -205,6 +206,40 @@ spmv_batched_csr_xs(const mgb_csr_batch_item* __restrict__ items, int64_t nitems
   }
 }
 
+// One CTA per matrix at a time with x read through L1 (configs >= BAT_FIRST_XL1):
+// the CTA's warps share one matrix, so its x (up to a few tens of KB) stays
+// in L1 while they work on it; no staging, no wait.
+template <typename T, int CFG>
+__global__ void __launch_bounds__(BAT_WARPS * 32, 3)
+spmv_batched_csr_xl1(const mgb_csr_batch_item* __restrict__ items, int64_t nitems, int32_t* ws, int init) {
+  constexpr int SEG = BAT_SEG[CFG];
+  constexpr int64_t CPW = BAT_XS_CPW[CFG];
+  __shared__ csr::WarpStage<T, SEG> stage[BAT_WARPS];
+  __shared__ int s_q;
+  const int lane = threadIdx.x & 31;
+  const int w = threadIdx.x >> 5;
+  if (ws[2] != CFG) {
+    if (threadIdx.x == 0) ws[3] = 1;
+    return;
+  }
+  const int32_t* __restrict__ order = ws + BAT_HEADER;
+  while (true) {
+    if (threadIdx.x == 0) s_q = atomicAdd(ws, 1);
+    __syncthreads();
+    const int q = s_q;
+    __syncthreads();
+    if (q >= nitems) break;
+    const mgb_csr_batch_item it = items[__ldg(order + q)];
+    int64_t chunk = (it.nnz + BAT_WARPS * CPW - 1) / (BAT_WARPS * CPW);
+    chunk = chunk < 256 ? 256 : (chunk > 4096 ? 4096 : chunk);
+    const int64_t nch = it.nnz / chunk + 1;
+    for (int64_t c = w; c < nch; c += BAT_WARPS)
+      csr::csr_chunk_x<T, SEG>(c, chunk, it.nrows, it.ncols, it.row_offsets, it.column_indices,
+                               static_cast<const T*>(it.values), csr::XGlobal<T>{static_cast<const T*>(it.x)},
+                               static_cast<T*>(it.y), init, stage[w], lane);
+  }
+}
+
 // order keys: (INT32_MAX - nnz) << 32 | index, so an ascending sort puts the
 // largest matrices first (longest-processing-time-first scheduling)
 __global__ void batch_order_keys(const mgb_csr_batch_item* __restrict__ items, int64_t n, uint64_t* keys) {
@@ -270,7 +305,9 @@ int plan(const mgb_csr_batch_item* items, int64_t nitems, int config, void* work
 
 template <typename T, int CFG>
 int launch_cfg(const mgb_csr_batch_item* items, int64_t nitems, int32_t* ws, int init, cudaStream_t s) {
-  if constexpr (CFG >= BAT_FIRST_XS) {
+  if constexpr (CFG >= BAT_FIRST_XL1) {
+    spmv_batched_csr_xl1<T, CFG><<<num_sms() * 3, BAT_WARPS * 32, 0, s>>>(items, nitems, ws, init);
+  } else if constexpr (CFG >= BAT_FIRST_XS) {
     constexpr size_t smem = 2 * BAT_XS_BYTES + BAT_WARPS * sizeof(csr::WarpStage<T, BAT_SEG[CFG]>);
     // set once per device (a function attribute, not a stream operation)
     static bool attr_set[64] = {};
@@ -304,7 +341,9 @@ int launch(const mgb_csr_batch_item* items, int64_t nitems, int config, void* wo
     case 4: return launch_cfg<T, 4>(items, nitems, ws, init, s);
     case 5: return launch_cfg<T, 5>(items, nitems, ws, init, s);
     case 6: return launch_cfg<T, 6>(items, nitems, ws, init, s);
-    default: return launch_cfg<T, 7>(items, nitems, ws, init, s);
+    case 7: return launch_cfg<T, 7>(items, nitems, ws, init, s);
+    case 8: return launch_cfg<T, 8>(items, nitems, ws, init, s);
+    default: return launch_cfg<T, 9>(items, nitems, ws, init, s);
   }
 }
 

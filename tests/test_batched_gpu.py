@@ -33,7 +33,7 @@ def check(mats, xs, ys, y0s, init, tol):
         assert rel_err(y.cpu().numpy(), ref) <= tol
 
 
-@pytest.mark.parametrize("config", range(8))
+@pytest.mark.parametrize("config", range(10))
 def test_every_config(cuda, config):
     mats, dev, xs, ys, _ = make_batch(60, seed=config)
     y0s = [y.cpu().numpy() for y in ys]
