@@ -624,7 +624,8 @@ def run_gpu_batched(args, rank: int, world: int, local_rank: int):
                    "autotune_ms_per_config": tune_ms},
         "pct_hbm_peak": 100.0 * achieved / peak, "rel_err_vs_oracle": check_err,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "peak_source": peak_src, "algorithmic_bytes_per_launch": nbytes},
+                     "traffic": batched_traffic(args), "peak_source": peak_src,
+                     "algorithmic_bytes_per_launch": nbytes},
         "separate_calls": {"ms": sep_ms, "GB/s": nbytes / (sep_ms * 1e-3) / 1e9, "launches": 2 * len(mats),
                            "speedup_of_batched": sep_ms / kernel_ms},
         "e2e": {"value": world * nbytes / (e2e_ms * 1e-3) / 1e9, "unit": "GB/s", "h2d_bytes_per_step": h2d,
@@ -659,6 +660,23 @@ def launches_per_step(hm) -> int:
     if f == 4:
         return 1 + (2 if hm["coo"]["nnz"] else 0)
     return 1
+
+
+def batched_traffic(args):
+    """DRAM bytes per launch of the batched kernel from its committed ncu
+    summary (the default 4,096-matrix FP64 batch only)."""
+    if args.batch != 4096 or args.dtype != "f64":
+        return None
+    p = os.path.join(ROOT, "profiles", "spmv_batched_csr_f64.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("dram_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip().split()[0])
+            except ValueError:
+                return None
+    return None
 
 
 def profile_traffic(args):
