@@ -54,3 +54,29 @@ def test_empty_matrix_is_a_noop_without_gpu(lib_built):
     lib = _lib.load()
     d = _lib.Csr(0, 0, 0, None, None, None)
     assert lib.mgb_spmv_csr_f64(C.byref(d), None, None, 1, None) == 0
+
+
+def test_size_limits_rejected_before_any_device_work(lib_built):
+    """int32 indices: matrices past the limits are refused up front
+    (MGB_ERR_INVALID_INPUT) instead of overflowing inside a kernel."""
+    lib = _lib.load()
+    fake = C.c_void_p(16)  # never dereferenced: the size checks come first
+    big = _lib.Csr(10, 10, (1 << 31) - 100, fake, fake, fake)
+    assert lib.mgb_spmv_csr_f64(C.byref(big), fake, fake, 1, None) == 3
+    assert lib.mgb_spmv_csr_variant_f64(C.byref(big), fake, fake, 1, 2, None) == 3
+    coo = _lib.Coo(1 << 31, 10, 5, fake, fake, fake)
+    assert lib.mgb_spmv_coo_f64(C.byref(coo), fake, fake, 1, None) == 3
+    bad_variant = _lib.Csr(10, 10, 5, fake, fake, fake)
+    assert lib.mgb_spmv_csr_variant_f64(C.byref(bad_variant), fake, fake, 1, 7, None) == 8
+    out = C.c_int64()
+    assert lib.mgb_spmv_csr_host_workspace_bytes(C.byref(bad_variant), 3, C.byref(out)) == 8
+    assert lib.mgb_spmv_csr_host_workspace_bytes(C.byref(bad_variant), 8, C.byref(out)) == 0 and out.value > 0
+
+
+def test_null_pointers_with_nonempty_sizes_rejected(lib_built):
+    lib = _lib.load()
+    d = _lib.Csr(10, 10, 5, None, None, None)
+    assert lib.mgb_spmv_csr_f64(C.byref(d), None, None, 1, None) == 8
+    assert lib.mgb_spmv_dot_csr_f64(C.byref(d), None, None, 1, 1, None, None) == 8
+    coo = _lib.Coo(10, 10, 5, None, None, None)
+    assert lib.mgb_spmv_coo_f64(C.byref(coo), None, None, 1, None) == 8

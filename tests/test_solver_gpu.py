@@ -153,3 +153,16 @@ def test_cg_rejects_non_spd_and_nonsquare(cuda):
     with pytest.raises(mgb.InvalidInputException):
         solvers.cg(B, torch.zeros(40, dtype=torch.float64, device="cuda"),
                    torch.zeros(40, dtype=torch.float64, device="cuda"))
+
+
+def test_cg_f32(cuda):
+    hm = gen.laplacian_2d(60, dtype=np.float32)
+    n = hm["nrows"]
+    b = gen.x_vector(n, seed=18, dtype=np.float32)
+    A = mgb.matrix_from_host(hm, device="cuda")
+    x = torch.zeros(n, dtype=torch.float32, device="cuda")
+    it, res = solvers.cg(A, torch.from_numpy(b).cuda(), x, max_iters=2000, rtol=1e-5)
+    assert 0 < it < 2000 and res <= 1e-5
+    h64 = dict(hm, values=hm["values"].astype(np.float64))
+    true = b.astype(np.float64) - O.OracleMatrix.from_host(h64).multiply(x.double().cpu().numpy())
+    assert np.linalg.norm(true) <= 1e-4 * np.linalg.norm(b)
