@@ -23,6 +23,8 @@
 
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
+#include <cstring>
 #include <stdexcept>
 #include <string>
 #include <type_traits>
@@ -934,6 +936,75 @@ CgResult cg(const CsrMatrix<T>& A, const DenseVector<T>& b, DenseVector<T>& x, i
                                      &r.relative_residual),
               "cg<GB300>");
   return r;
+}
+
+// ------------------------------------------------------------- selector ---
+// The learned format selector (an extension: the reference picks a format
+// with the --morpheus-format flag, impl/Morpheus_Core.cpp:101-125).  Loads
+// morpheus_gb300/selector_weights.bin (magic "MGBSEL01", u32 version, u32
+// parameter count, u32 metadata length, mu[12], sigma[12], parameters,
+// metadata; little-endian float32), computes the 12 features of the matrix
+// on the GPU and runs the network's forward kernel; infeasible formats are
+// never chosen.
+class FormatSelector {
+ public:
+  explicit FormatSelector(const std::string& weights_path) {
+    std::FILE* f = std::fopen(weights_path.c_str(), "rb");
+    if (!f) throw IOException("cannot open " + weights_path);
+    char magic[8];
+    uint32_t head[3];
+    const int n = mgb_mlp_num_params();
+    std::vector<float> mu(12), sigma(12), params((size_t)n);
+    const bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, "MGBSEL01", 8) == 0 &&
+                    std::fread(head, 4, 3, f) == 3 && head[0] == 1 && (int)head[1] == n &&
+                    std::fread(mu.data(), 4, 12, f) == 12 && std::fread(sigma.data(), 4, 12, f) == 12 &&
+                    std::fread(params.data(), 4, (size_t)n, f) == (size_t)n;
+    std::fclose(f);
+    if (!ok) throw IOException(weights_path + ": not a selector weights file of this library");
+    for (auto& v : sigma) v = v < 1e-6f ? 1e-6f : v;
+    params_.assign(params);
+    mu_.assign(mu);
+    sigma_.assign(sigma);
+  }
+
+  // The format the network picks for A (any container; non-CSR containers
+  // are converted to CSR on the device for the features).
+  template <class Matrix>
+  formats_e select(const Matrix& A) const {
+    using T = typename Matrix::value_type;
+    CsrMatrix<T> csr;
+    Impl::from_coo(Impl::to_coo(A), csr);
+    return select_csr(csr);
+  }
+  template <class T>
+  formats_e select(const CsrMatrix<T>& A) const { return select_csr(A); }
+
+ private:
+  template <class T>
+  formats_e select_csr(const CsrMatrix<T>& A) const {
+    std::vector<float> feat(12);
+    std::vector<uint8_t> feas(6);
+    mgb_csr d = A.desc();
+    Impl::check(mgb_features_csr(&d, feat.data(), feas.data(), nullptr), "FormatSelector::select");
+    DeviceArray<float> X(feat), logp(6);
+    DeviceArray<uint8_t> F(feas);
+    Impl::check(mgb_mlp_forward_f32(params_.data(), mu_.data(), sigma_.data(), X.data(), F.data(), 1, logp.data(),
+                                    nullptr),
+                "FormatSelector::select");
+    const std::vector<float> lp = logp.to_host();
+    int best = CSR_FORMAT;
+    for (int k = 0; k < 6; k++)
+      if (feas[k] && (!feas[best] || lp[k] > lp[best])) best = k;
+    return (formats_e)best;
+  }
+  DeviceArray<float> params_, mu_, sigma_;
+};
+
+// In-place switch of a DynamicMatrix to the format the selector picks.
+template <class ExecSpace, class ValueType>
+conversion_error_e convert(DynamicMatrix<ValueType>& A, const FormatSelector& selector) {
+  const formats_e f = std::visit([&](const auto& m) { return selector.select(m); }, A.const_formats());
+  return convert<ExecSpace>(A, f);
 }
 
 }  // namespace Morpheus

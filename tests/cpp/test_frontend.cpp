@@ -489,10 +489,53 @@ void test_solver() {
   expect(std::sqrt(num / den) <= 1e-9, "cg: true residual against the oracle multiply");
 }
 
+// the learned selector from C++: a stencil goes to a diagonal format, a
+// power-law-like matrix stays row-based, and the switch keeps the product
+void test_selector(const std::string& weights) {
+  const Morpheus::FormatSelector sel(weights);
+  const int64_t n = 40;  // 40^3 7-point stencil
+  HostCsr<double> h;
+  h.n = n * n * n;
+  h.ro.push_back(0);
+  for (int64_t i = 0; i < n; i++)
+    for (int64_t j = 0; j < n; j++)
+      for (int64_t k = 0; k < n; k++) {
+        const int64_t r = (i * n + j) * n + k;
+        const int64_t nb[7][3] = {{-1, 0, 0}, {0, -1, 0}, {0, 0, -1}, {0, 0, 0}, {0, 0, 1}, {0, 1, 0}, {1, 0, 0}};
+        for (const auto& d : nb) {
+          const int64_t a = i + d[0], b = j + d[1], c = k + d[2];
+          if (a < 0 || a >= n || b < 0 || b >= n || c < 0 || c >= n) continue;
+          h.ci.push_back((int32_t)((a * n + b) * n + c));
+          h.v.push_back(d[0] == 0 && d[1] == 0 && d[2] == 0 ? 6.0 : -1.0);
+        }
+        (void)r;
+        h.ro.push_back((int32_t)h.ci.size());
+      }
+  const Morpheus::CsrMatrix<double> A(h.n, h.n, h.ro, h.ci, h.v);
+  const Morpheus::formats_e f = sel.select(A);
+  expect(f >= Morpheus::COO_FORMAT && f < Morpheus::NFORMATS, "selector returns a format");
+  Morpheus::DynamicMatrix<double> dyn(A);
+  expect(Morpheus::convert<GB300>(dyn, sel) == Morpheus::CONV_SUCCESS && dyn.active_index() == f,
+         "convert(dyn, selector) switches to the selected format");
+  const std::vector<double> xh = host_vector<double>(h.n, 31);
+  Morpheus::DenseVector<double> x(xh), y(h.n), y2(h.n);
+  Morpheus::multiply<GB300>(dyn, x, y);
+  Morpheus::multiply<GB300>(A, x, y2);
+  expect(rel_err(y.to_host(), y2.to_host()) <= 1e-12, "multiply after the selector's switch");
+  bool threw = false;
+  try {
+    Morpheus::FormatSelector bad("/nonexistent/weights.bin");
+  } catch (const Morpheus::IOException&) {
+    threw = true;
+  }
+  expect(threw, "missing weights file throws IOException");
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
   const std::string dir = argc > 1 ? argv[1] : ".";
+  const std::string weights = argc > 2 ? argv[2] : "";
   try {
     for (int64_t n : {10, 100, 1000}) {
       test_banded<double>(n);
@@ -505,6 +548,7 @@ int main(int argc, char** argv) {
     test_vector_ops<float>();
     test_matrix_market(dir);
     test_solver();
+    if (!weights.empty()) test_selector(weights);
   } catch (const std::exception& e) {
     std::printf("FAIL: unexpected exception: %s\n", e.what());
     return 2;

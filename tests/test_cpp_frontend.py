@@ -41,6 +41,7 @@ def test_frontend_compiles_and_links(lib_built, oracle_built, tmp_path):
 @pytest.mark.gpu
 def test_frontend_on_gpu(cuda, oracle_built, lib_built, tmp_path):
     exe = _build(str(tmp_path / "test_frontend"), lib_built, oracle_built)
-    r = subprocess.run([exe, str(tmp_path)], capture_output=True, text=True, timeout=600)
+    weights = os.path.join(ROOT, "morpheus_gb300", "selector_weights.bin")
+    r = subprocess.run([exe, str(tmp_path), weights], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout[-4000:] + r.stderr[-2000:]
     assert ", 0 failed" in r.stdout
