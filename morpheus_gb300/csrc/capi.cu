@@ -1,5 +1,6 @@
 // capi.cu -- library-level entry points: status names, version, CUDA error
 // bookkeeping and the cached device query.
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 
@@ -16,17 +17,19 @@ int record_cuda_error(cudaError_t e) {
 }
 
 int num_sms() {
-  static int cache[64] = {0};
+  // per-device cache; atomics because several host threads may call at once
+  static std::atomic<int> cache[64];
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return 152;
-  if (dev < 0 || dev >= 64) dev = 0;
-  if (cache[dev] == 0) {
-    int n = 0;
-    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
-      n = 152;
-    cache[dev] = n;
+  const bool cacheable = dev >= 0 && dev < 64;
+  if (cacheable) {
+    const int c = cache[dev].load(std::memory_order_relaxed);
+    if (c > 0) return c;
   }
-  return cache[dev];
+  int n = 0;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 152;
+  if (cacheable) cache[dev].store(n, std::memory_order_relaxed);
+  return n;
 }
 
 }  // namespace mgb

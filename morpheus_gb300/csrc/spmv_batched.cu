@@ -24,6 +24,8 @@
 // chunk-queue kernel); the next matrix's x is copied by TMA while the CTA
 // works on the current one.  mgb_spmv_batched_csr_autotune_* times every
 // configuration on the actual batch with CUDA events and returns the fastest.
+#include <atomic>
+
 #include "csr_chunk.cuh"
 #include "primitives.cuh"
 
@@ -310,13 +312,13 @@ int launch_cfg(const mgb_csr_batch_item* items, int64_t nitems, int32_t* ws, int
   } else if constexpr (CFG >= BAT_FIRST_XS) {
     constexpr size_t smem = 2 * BAT_XS_BYTES + BAT_WARPS * sizeof(csr::WarpStage<T, BAT_SEG[CFG]>);
     // set once per device (a function attribute, not a stream operation)
-    static bool attr_set[64] = {};
+    static std::atomic<bool> attr_set[64];
     int dev = 0;
     MGB_CUDA_CHECK(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= 64 || !attr_set[dev]) {
+    if (dev < 0 || dev >= 64 || !attr_set[dev].load(std::memory_order_acquire)) {
       MGB_CUDA_CHECK(cudaFuncSetAttribute(spmv_batched_csr_xs<T, CFG>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      if (dev >= 0 && dev < 64) attr_set[dev] = true;
+      if (dev >= 0 && dev < 64) attr_set[dev].store(true, std::memory_order_release);
     }
     spmv_batched_csr_xs<T, CFG><<<num_sms() * 2, BAT_WARPS * 32, smem, s>>>(items, nitems, ws, init);
   } else {
