@@ -384,6 +384,12 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
             else pinned[id(hm["values"])]
         e2e_api = "multiply_host (mgb_spmv_csr_host, pipelined row blocks)"
         mgb.multiply_host(host_csr, xh, yh, init=True)  # warm-up (pool allocation, kernel choice)
+    else:
+        for h, d in pairs:  # one untimed end-to-end step (allocator pool, first-touch costs)
+            d.copy_(h, non_blocking=True)
+        x.copy_(xh, non_blocking=True)
+        mgb.multiply(dev_bufs, x, y, init=True)
+        yh.copy_(y, non_blocking=True)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
