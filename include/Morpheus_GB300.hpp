@@ -233,19 +233,29 @@ class CsrMatrix {  // core/src/Morpheus_CsrMatrix.hpp:533-537
   void resize(int64_t r, int64_t c, int64_t n) {
     nrows_ = r; ncols_ = c; nnz_ = n;
     ro_.resize(r + 1); ci_.resize(n); v_.resize(n);
-    variant_ = 0;
+    forget_kernel_variant();
   }
-  // SpMV kernel of this matrix (MGB_CSR_ROWS or MGB_CSR_SEGMENTS), measured
-  // on the device at the first multiply and cached.  Call
-  // forget_kernel_variant() after writing new row offsets.
+  // SpMV kernel of this matrix (MGB_CSR_ROWS, MGB_CSR_SEGMENTS or
+  // MGB_CSR_SPLIT), measured on the device at the first multiply and cached,
+  // and for the lane-segment kernel its chunk plan (mgb_csr_plan).  Both
+  // depend on the row offsets only: the non-const row_offsets() accessor and
+  // resize() drop them; call forget_kernel_variant() after writing new row
+  // offsets through a pointer kept from earlier.
   int kernel_variant() const;
-  void forget_kernel_variant() { variant_ = 0; }
+  const int32_t* chunk_plan(int64_t* entries) const;
+  void forget_kernel_variant() {
+    variant_ = 0;
+    plan_ok_ = false;
+  }
   int64_t nrows() const { return nrows_; }
   int64_t ncols() const { return ncols_; }
   int64_t nnnz() const { return nnz_; }
   formats_e format_enum() const { return format; }
   int format_index() const { return format; }
-  DeviceArray<int32_t>& row_offsets() { return ro_; }
+  DeviceArray<int32_t>& row_offsets() {
+    forget_kernel_variant();
+    return ro_;
+  }
   DeviceArray<int32_t>& column_indices() { return ci_; }
   DeviceArray<ValueType>& values() { return v_; }
   const DeviceArray<int32_t>& crow_offsets() const { return ro_; }
@@ -261,6 +271,8 @@ class CsrMatrix {  // core/src/Morpheus_CsrMatrix.hpp:533-537
   DeviceArray<int32_t> ro_, ci_;
   DeviceArray<ValueType> v_;
   mutable int variant_ = 0;
+  mutable DeviceArray<int32_t> plan_;
+  mutable bool plan_ok_ = false;
 };
 
 template <class ValueType>
@@ -272,6 +284,20 @@ int CsrMatrix<ValueType>::kernel_variant() const {
     variant_ = v;
   }
   return variant_;
+}
+
+template <class ValueType>
+const int32_t* CsrMatrix<ValueType>::chunk_plan(int64_t* entries) const {
+  mgb_csr d = desc();
+  int64_t n = 0;
+  Impl::check(mgb_csr_plan_entries(&d, &n), "CsrMatrix::chunk_plan");
+  if (!plan_ok_ || (int64_t)plan_.size() != n) {
+    plan_.resize((size_t)n);
+    Impl::check(mgb_csr_plan(&d, plan_.data(), n, nullptr), "CsrMatrix::chunk_plan");
+    plan_ok_ = true;
+  }
+  *entries = n;
+  return plan_.data();
 }
 
 template <class ValueType>
@@ -464,6 +490,9 @@ template <> struct Suffix<double> {
   static int csr(const mgb_csr* a, const double* x, double* y, int i, int v, void* s) {
     return mgb_spmv_csr_variant_f64(a, x, y, i, v, s);
   }
+  static int csr_planned(const mgb_csr* a, const int32_t* p, int64_t n, const double* x, double* y, int i, void* s) {
+    return mgb_spmv_csr_planned_f64(a, p, n, x, y, i, s);
+  }
   static int coo(const mgb_coo* a, const double* x, double* y, int i, void* s) { return mgb_spmv_coo_f64(a, x, y, i, s); }
   static int dia(const mgb_dia* a, const double* x, double* y, int i, void* s) { return mgb_spmv_dia_f64(a, x, y, i, s); }
   static int ell(const mgb_ell* a, const double* x, double* y, int i, void* s) { return mgb_spmv_ell_f64(a, x, y, i, s); }
@@ -478,6 +507,9 @@ template <> struct Suffix<double> {
 template <> struct Suffix<float> {
   static int csr(const mgb_csr* a, const float* x, float* y, int i, int v, void* s) {
     return mgb_spmv_csr_variant_f32(a, x, y, i, v, s);
+  }
+  static int csr_planned(const mgb_csr* a, const int32_t* p, int64_t n, const float* x, float* y, int i, void* s) {
+    return mgb_spmv_csr_planned_f32(a, p, n, x, y, i, s);
   }
   static int coo(const mgb_coo* a, const float* x, float* y, int i, void* s) { return mgb_spmv_coo_f32(a, x, y, i, s); }
   static int dia(const mgb_dia* a, const float* x, float* y, int i, void* s) { return mgb_spmv_dia_f32(a, x, y, i, s); }
@@ -494,7 +526,14 @@ template <> struct Suffix<float> {
 template <class T>
 void spmv(const CsrMatrix<T>& A, const T* x, T* y, bool init) {
   auto d = A.desc();
-  check(Suffix<T>::csr(&d, x, y, init, A.kernel_variant(), nullptr), "multiply<GB300>(CsrMatrix)");
+  const int v = A.kernel_variant();
+  if (v == MGB_CSR_SEGMENTS) {
+    int64_t n = 0;
+    const int32_t* plan = A.chunk_plan(&n);
+    check(Suffix<T>::csr_planned(&d, plan, n, x, y, init, nullptr), "multiply<GB300>(CsrMatrix)");
+  } else {
+    check(Suffix<T>::csr(&d, x, y, init, v, nullptr), "multiply<GB300>(CsrMatrix)");
+  }
 }
 template <class T>
 void spmv(const CooMatrix<T>& A, const T* x, T* y, bool init) {

@@ -139,6 +139,26 @@ int mgb_csr_choose_kernel(const mgb_csr* A, int* variant, void* stream);
 int mgb_spmv_csr_variant_f64(const mgb_csr* A, const double* x, double* y, int init, int variant, void* stream);
 int mgb_spmv_csr_variant_f32(const mgb_csr* A, const float* x, float* y, int init, int variant, void* stream);
 
+/* Chunk plan of the lane-segment kernel (MGB_CSR_SEGMENTS).  The reference
+ * has no plan: its CSR kernels map rows to threads directly
+ * (impl/Csr/Kernels/Morpheus_Multiply_Impl.hpp:36-168).  Each warp of the
+ * lane-segment kernel otherwise finds its rows with two searches over
+ * row_offsets on every call; the plan stores the first row of every warp
+ * chunk, int32 entries = mgb_csr_plan_entries, so that a multiply reads two
+ * integers instead.  It depends on nrows, nnz, row_offsets and the GPU it was
+ * made on, not on values or x: make it once per matrix structure (one light
+ * kernel, asynchronous) and pass it to every planned multiply with that
+ * structure.  Same y, bit for bit, as mgb_spmv_csr_variant_* with
+ * MGB_CSR_SEGMENTS.  A plan of the wrong size is MGB_ERR_BAD_ARGUMENT; a plan
+ * made for another structure of the same size gives wrong sums but reads
+ * nothing outside the matrix. */
+int mgb_csr_plan_entries(const mgb_csr* A, int64_t* entries);
+int mgb_csr_plan(const mgb_csr* A, int32_t* plan, int64_t entries, void* stream);
+int mgb_spmv_csr_planned_f64(const mgb_csr* A, const int32_t* plan, int64_t entries, const double* x, double* y,
+                             int init, void* stream);
+int mgb_spmv_csr_planned_f32(const mgb_csr* A, const int32_t* plan, int64_t entries, const float* x, float* y,
+                             int init, void* stream);
+
 /* replaces impl/Coo/Cuda/Morpheus_Multiply_Impl.hpp:50-176.  Like the
  * reference's CUDA path, A must be sorted by row (columns in any order). */
 int mgb_spmv_coo_f64(const mgb_coo* A, const double* x, double* y, int init, void* stream);

@@ -74,6 +74,9 @@ for _dt, _ct in (("f64", C.c_double), ("f32", C.c_float)):
 _SIGS["mgb_csr_choose_kernel"] = (C.c_int, [C.POINTER(Csr), C.POINTER(C.c_int), vp])
 for _dt in ("f64", "f32"):
     _SIGS[f"mgb_spmv_csr_variant_{_dt}"] = (C.c_int, [C.POINTER(Csr), vp, vp, C.c_int, C.c_int, vp])
+    _SIGS[f"mgb_spmv_csr_planned_{_dt}"] = (C.c_int, [C.POINTER(Csr), vp, i64, vp, vp, C.c_int, vp])
+_SIGS["mgb_csr_plan_entries"] = (C.c_int, [C.POINTER(Csr), C.POINTER(i64)])
+_SIGS["mgb_csr_plan"] = (C.c_int, [C.POINTER(Csr), vp, i64, vp])
 _SIGS["mgb_analytics_csr"] = (C.c_int, [C.POINTER(Csr), C.POINTER(C.c_double), vp])
 _SIGS["mgb_count_nnz_per_row_csr"] = (C.c_int, [C.POINTER(Csr), vp, C.c_int, vp])
 _SIGS["mgb_count_nnz_per_row_coo"] = (C.c_int, [C.POINTER(Coo), vp, C.c_int, vp])

@@ -70,9 +70,15 @@ def multiply(A: _Matrix, x, y, init: bool = True, stream=None) -> None:
     if xt.numel() < A.ncols() or yt.numel() < A.nrows():
         raise InvalidInputException("x or y too short for A")
     desc = A._desc()
-    if A.FORMAT == CSR_FORMAT:  # cached per matrix: row-tile or lane-segment kernel
-        _lib.call(f"mgb_spmv_csr_variant_{_suffix(A.dtype)}", C.byref(desc), C.c_void_p(xt.data_ptr()),
-                  C.c_void_p(yt.data_ptr()), 1 if init else 0, A.kernel_variant(), _stream_handle(stream))
+    if A.FORMAT == CSR_FORMAT:  # cached per matrix: kernel choice, and the chunk plan of the lane-segment kernel
+        variant, sh = A.kernel_variant(), _stream_handle(stream)
+        if variant == CSR_SEGMENTS:
+            plan, entries = A.chunk_plan(sh)
+            _lib.call(f"mgb_spmv_csr_planned_{_suffix(A.dtype)}", C.byref(desc), C.c_void_p(plan.data_ptr()),
+                      entries, C.c_void_p(xt.data_ptr()), C.c_void_p(yt.data_ptr()), 1 if init else 0, sh)
+        else:
+            _lib.call(f"mgb_spmv_csr_variant_{_suffix(A.dtype)}", C.byref(desc), C.c_void_p(xt.data_ptr()),
+                      C.c_void_p(yt.data_ptr()), 1 if init else 0, variant, sh)
         return
     name = f"mgb_spmv_{_FMT_NAME[A.FORMAT]}_{_suffix(A.dtype)}"
     _lib.call(name, C.byref(desc), C.c_void_p(xt.data_ptr()), C.c_void_p(yt.data_ptr()),

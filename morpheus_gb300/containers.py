@@ -153,6 +153,7 @@ class CsrMatrix(_Matrix):
         if self._ro.numel() != self._nrows + 1 or self._ci.numel() != self._nnz or self._v.numel() != self._nnz:
             raise InvalidInputException("CSR arrays have the wrong sizes")
         self._variant = None
+        self._plan = None
 
     def row_offsets(self): return self._ro
     def column_indices(self): return self._ci
@@ -173,8 +174,25 @@ class CsrMatrix(_Matrix):
             self._variant = out.value
         return self._variant
 
+    def chunk_plan(self, stream=None) -> tuple[torch.Tensor, int]:
+        """(plan, entries): the first row of every warp chunk of the
+        lane-segment kernel (mgb_csr_plan), made once on `stream` (a raw
+        CUDA stream handle or None) and cached, so that multiplies skip the
+        row-offset searches.  Cleared with the kernel choice."""
+        if self._plan is None:
+            d = self._desc()
+            n = C.c_int64()
+            _lib.call("mgb_csr_plan_entries", C.byref(d), C.byref(n))
+            plan = torch.empty(n.value, dtype=torch.int32, device=self.device)
+            _lib.call("mgb_csr_plan", C.byref(d), C.c_void_p(plan.data_ptr()), n.value, stream)
+            self._plan = (plan, n.value)
+        return self._plan
+
     def forget_kernel_variant(self) -> None:
+        """Drops the cached kernel choice and chunk plan (call after writing
+        new row offsets in place)."""
         self._variant = None
+        self._plan = None
 
     def resize(self, nrows, ncols, nnz):
         self.__init__(nrows, ncols, nnz, dtype=self.dtype, device=self.device)

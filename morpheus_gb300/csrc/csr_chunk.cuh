@@ -61,25 +61,43 @@ struct XShared {
   __device__ __forceinline__ T operator()(int32_t c) const { return p[c]; }
 };
 
-// Processes warp chunk `wc` of one CSR matrix: the rows whose first entry lies
-// in [wc*chunk, (wc+1)*chunk).  Chunks are whole rows, so every y entry is
-// written by exactly one warp.  Returns the chunk's rows (their y entries are
-// visible to the whole warp after a __syncwarp()).  xl(c) reads x[c].
-template <typename T, int SEG, typename XL>
-__device__ __forceinline__ RowRange csr_chunk_x(int64_t wc, int64_t chunk, int64_t nrows, int64_t ncols,
-                                                const int32_t* __restrict__ ro, const int32_t* __restrict__ ci,
-                                                const T* __restrict__ va, XL xl, T* __restrict__ y, int init,
-                                                WarpStage<T, SEG>& stg, int lane) {
-  constexpr int CSR_PAD = SEG + 1;
-  T* sv = stg.val;
-  int32_t* sc = stg.col;
-  int32_t* sro = stg.ro;
-  // rows starting in [s0, s1)
+// Rows of warp chunk `wc`: those whose first entry lies in [wc*chunk,
+// (wc+1)*chunk), found by two 32-ary searches over the row offsets.
+__device__ __forceinline__ RowRange chunk_rows(int64_t wc, int64_t chunk, int64_t nrows,
+                                               const int32_t* __restrict__ ro, int lane) {
   const int64_t s0 = wc * chunk, s1 = s0 + chunk;
   int64_t r_begin = warp_lower_bound(ro, 0, nrows + 1, s0, lane);
   int64_t r_end = warp_lower_bound(ro, r_begin, nrows + 1, s1, lane);
   if (r_begin > nrows) r_begin = nrows;
   if (r_end > nrows) r_end = nrows;
+  return RowRange{r_begin, r_end};
+}
+
+// Rows of warp chunk `wc` read from a chunk plan: plan[k] = the first row
+// whose first entry is at or after k*chunk (nrows if none), k = 0..nchunks.
+// Values are clamped, so a plan made for another structure gives wrong
+// sums but no access outside the matrix.
+__device__ __forceinline__ RowRange planned_rows(int64_t wc, int64_t nrows, const int32_t* __restrict__ plan) {
+  int64_t r_begin = __ldg(plan + wc), r_end = __ldg(plan + wc + 1);
+  r_begin = r_begin < 0 ? 0 : (r_begin > nrows ? nrows : r_begin);
+  r_end = r_end < r_begin ? r_begin : (r_end > nrows ? nrows : r_end);
+  return RowRange{r_begin, r_end};
+}
+
+// Processes the rows [rows.begin, rows.end) of one warp chunk of a CSR
+// matrix.  Chunks are whole rows, so every y entry is written by exactly one
+// warp.  Returns the chunk's rows (their y entries are visible to the whole
+// warp after a __syncwarp()).  xl(c) reads x[c].
+template <typename T, int SEG, typename XL>
+__device__ __forceinline__ RowRange csr_rows_x(RowRange rows, int64_t nrows, int64_t ncols,
+                                               const int32_t* __restrict__ ro, const int32_t* __restrict__ ci,
+                                               const T* __restrict__ va, XL xl, T* __restrict__ y, int init,
+                                               WarpStage<T, SEG>& stg, int lane) {
+  constexpr int CSR_PAD = SEG + 1;
+  T* sv = stg.val;
+  int32_t* sc = stg.col;
+  int32_t* sro = stg.ro;
+  const int64_t r_begin = rows.begin, r_end = rows.end;
   if (r_begin >= r_end) return RowRange{r_begin, r_begin};
   const int64_t nr = r_end - r_begin;
   const bool staged = nr < CSR_RO_STAGE;  // offsets r_begin..r_end in smem
@@ -189,6 +207,17 @@ __device__ __forceinline__ RowRange csr_chunk_x(int64_t wc, int64_t chunk, int64
   const int64_t kprev = __shfl_up_sync(0xffffffffu, key, 1);
   if (hrow >= 0) y[hrow] = (lane > 0 && kprev == hrow) ? hval + vprev : hval;
   return RowRange{r_begin, r_end};
+}
+
+// Processes warp chunk `wc` of one CSR matrix: the rows whose first entry
+// lies in [wc*chunk, (wc+1)*chunk).
+template <typename T, int SEG, typename XL>
+__device__ __forceinline__ RowRange csr_chunk_x(int64_t wc, int64_t chunk, int64_t nrows, int64_t ncols,
+                                                const int32_t* __restrict__ ro, const int32_t* __restrict__ ci,
+                                                const T* __restrict__ va, XL xl, T* __restrict__ y, int init,
+                                                WarpStage<T, SEG>& stg, int lane) {
+  return csr_rows_x<T, SEG>(chunk_rows(wc, chunk, nrows, ro, lane), nrows, ncols, ro, ci, va, xl, y, init, stg,
+                            lane);
 }
 
 template <typename T, int64_t CHUNK, int SEG>

@@ -58,13 +58,14 @@ template <typename T>
 int launch_ell(const mgb_ell* A, const T* x, T* y, int init, cudaStream_t s);
 template <typename T>
 int launch_coo(const mgb_coo* A, const T* x, T* y, int init, cudaStream_t s);
-// CSR SpMV with an explicit kernel (MGB_CSR_SEGMENTS / MGB_CSR_ROWS).  With
-// partials != nullptr the kernel also forms x[0..nrows) . y, one partial per
-// warp, *npartials of them; partials == nullptr with npartials != nullptr
-// only reports that count.
+// CSR SpMV with an explicit kernel (MGB_CSR_SEGMENTS / MGB_CSR_ROWS /
+// MGB_CSR_SPLIT).  With partials != nullptr the kernel also forms
+// x[0..nrows) . y, one partial per warp, *npartials of them; partials ==
+// nullptr with npartials != nullptr only reports that count.  plan: an
+// optional chunk plan of plan_entries entries (lane-segment kernel only).
 template <typename T>
 int launch_csr_dot(const mgb_csr* A, const T* x, T* y, int init, void* stream, int variant, T* partials,
-                   int64_t* npartials);
+                   int64_t* npartials, const int32_t* plan = nullptr, int64_t plan_entries = 0);
 template <typename T>
 int launch_csr_rows(const mgb_csr* A, const T* x, T* y, int init, cudaStream_t s, T* partials = nullptr,
                     int64_t* npartials = nullptr);

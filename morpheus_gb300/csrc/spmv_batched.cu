@@ -18,12 +18,14 @@
 // per lane per step, the "vector width" of the staging loads) form six
 // chunk-queue configurations.  Two more configurations give each CTA a whole
 // matrix at a time (largest first): the CTA copies the matrix's x into
-// shared memory (up to 32 KB) and its warps split the matrix into
-// nnz-balanced chunks, so the random x reads become shared-memory reads
+// shared memory (up to 64 KB) with cp.async and its warps split the matrix
+// into nnz-balanced chunks, so the random x reads become shared-memory reads
 // instead of one L1TEX sector per nonzero (the unit that binds the
-// chunk-queue kernel); the next matrix's x is copied by TMA while the CTA
-// works on the current one.  mgb_spmv_batched_csr_autotune_* times every
-// configuration on the actual batch with CUDA events and returns the fastest.
+// chunk-queue kernel); with two buffers the next matrix's x is copied while
+// the CTA works on the current one.  Two last configurations also give each
+// CTA a whole matrix but read x through L1.  mgb_spmv_batched_csr_autotune_*
+// times every configuration on the actual batch with CUDA events and returns
+// the fastest.
 #include <atomic>
 
 #include "csr_chunk.cuh"
@@ -41,7 +43,7 @@ constexpr int BAT_FIRST_XL1 = 8;  // configurations 8, 9: matrix per CTA, x thro
 constexpr int64_t BAT_CHUNK[BAT_NCONFIGS] = {512, 1024, 2048, 4096, 1024, 2048, 0, 0, 0, 0};
 constexpr int BAT_SEG[BAT_NCONFIGS] = {8, 8, 8, 8, 4, 4, 8, 8, 8, 8};
 constexpr int BAT_XS_CPW[BAT_NCONFIGS] = {0, 0, 0, 0, 0, 0, 1, 2, 1, 2};  // chunks per warp
-constexpr int BAT_XS_BYTES = 32 * 1024;  // per x buffer, two buffers (larger x: read from global)
+constexpr int BAT_XS_BYTES = 64 * 1024;  // per x buffer (larger x: read from global)
 // workspace: int32 header[4] = {work counter, total work items, planned
 // config, error flag}, then int32[nitems + 1]: the chunk prefix (chunk-queue
 // configs) or the matrix order, largest nnz first (matrix-per-CTA configs)
@@ -94,24 +96,44 @@ spmv_batched_csr(const mgb_csr_batch_item* __restrict__ items, int64_t nitems, i
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
 
+// Starts the copy of x[0, n) into shared memory at xs with cp.async (no
+// registers held, every copy of the CTA in flight at once): 16-byte pieces
+// when x is 16-byte aligned, otherwise one element per copy.
+template <typename T>
+__device__ __forceinline__ void copy_x_async(T* xs, const T* __restrict__ xg, int64_t n) {
+  int64_t done = 0;
+  if ((reinterpret_cast<uintptr_t>(xg) & 15u) == 0) {
+    constexpr int64_t V = 16 / sizeof(T);
+    const int64_t nv = n / V;
+    for (int64_t i = threadIdx.x; i < nv; i += blockDim.x)
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_u32(xs + i * V)), "l"(xg + i * V)
+                   : "memory");
+    done = nv * V;
+  }
+  for (int64_t i = done + threadIdx.x; i < n; i += blockDim.x)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(smem_u32(xs + i)), "l"(xg + i),
+                 "n"((int)sizeof(T))
+                 : "memory");
+}
+
 // One CTA per matrix at a time, x in shared memory (configs >= BAT_FIRST_XS).
-// x of the next matrix streams into the second buffer by one TMA bulk copy
-// (cp.async.bulk, completion on an mbarrier) while the CTA works on the
-// current one.  The waits are bounded: a copy that never lands sets the
-// workspace error flag to 2 and the CTA leaves after a second bounded wait.
-template <typename T, int CFG>
-__global__ void __launch_bounds__(BAT_WARPS * 32, 2)
+// Each CTA takes the next matrix (largest first), copies its x (up to
+// BAT_XS_BYTES) into shared memory with cp.async, and its warps split the
+// matrix into nnz-balanced chunks whose random x reads are shared-memory
+// reads.  With NBUF = 2 the copy of the next matrix's x is in flight while
+// the CTA works on the current one (one CTA of 16 warps per SM); with NBUF =
+// 1 two CTAs of 8 warps share an SM, and one computes while the other
+// copies.  A wider x is read from global memory.  No thread waits on another
+// CTA, so there is no spin-wait.
+template <typename T, int CFG, int NBUF, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32, 16 / WARPS)
 spmv_batched_csr_xs(const mgb_csr_batch_item* __restrict__ items, int64_t nitems, int32_t* ws, int init) {
   constexpr int SEG = BAT_SEG[CFG];
   constexpr int64_t CPW = BAT_XS_CPW[CFG];
   constexpr int64_t XCAP = BAT_XS_BYTES / sizeof(T);  // entries per x buffer
   extern __shared__ __align__(16) unsigned char bat_smem[];
-  T* const xbuf0 = reinterpret_cast<T*>(bat_smem);
-  T* const xbuf1 = reinterpret_cast<T*>(bat_smem + BAT_XS_BYTES);
-  csr::WarpStage<T, SEG>* stage = reinterpret_cast<csr::WarpStage<T, SEG>*>(bat_smem + 2 * BAT_XS_BYTES);
+  csr::WarpStage<T, SEG>* stage = reinterpret_cast<csr::WarpStage<T, SEG>*>(bat_smem + NBUF * BAT_XS_BYTES);
   __shared__ int s_q[2];
-  __shared__ int s_xin[2];
-  __shared__ __align__(8) unsigned long long s_bar[2];
   const int lane = threadIdx.x & 31;
   const int w = threadIdx.x >> 5;
   if (ws[2] != CFG) {
@@ -119,83 +141,41 @@ spmv_batched_csr_xs(const mgb_csr_batch_item* __restrict__ items, int64_t nitems
     return;
   }
   const int32_t* __restrict__ order = ws + BAT_HEADER;
-  if (threadIdx.x == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&s_bar[0])) : "memory");
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&s_bar[1])) : "memory");
-    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-  }
-  __syncthreads();
-
-  // thread 0: take the next matrix and start its x copy into buffer `slot`;
-  // exactly one arrive on s_bar[slot] per call
-  auto fetch = [&](int slot) {
-    if (threadIdx.x != 0) return;
-    const int q = atomicAdd(ws, 1);
-    s_q[slot] = q;
-    T* dst = slot ? xbuf1 : xbuf0;
-    unsigned bytes = 0;
-    int xin = 0;
-    const T* xg = nullptr;
-    int64_t n = 0;
+  // takes the next matrix into slot b and starts the copy of its x into
+  // buffer b (one cp.async group per call, possibly empty)
+  auto fetch = [&](int b) {
+    if (threadIdx.x == 0) s_q[b] = atomicAdd(ws, 1);
+    __syncthreads();
+    const int q = s_q[b];
     if (q < nitems) {
       const mgb_csr_batch_item& it = items[__ldg(order + q)];
-      xg = static_cast<const T*>(it.x);
-      n = it.ncols;
-      xin = (n <= XCAP && n >= 0 && ((reinterpret_cast<uintptr_t>(xg) & 15u) == 0)) ? 1 : 0;
-      if (xin) bytes = (unsigned)(((uint64_t)n * sizeof(T)) & ~(uint64_t)15);
+      if (it.ncols <= XCAP)
+        copy_x_async(reinterpret_cast<T*>(bat_smem + b * BAT_XS_BYTES), static_cast<const T*>(it.x), it.ncols);
     }
-    s_xin[slot] = xin;
-    const unsigned bar = smem_u32(&s_bar[slot]);
-    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes) : "memory");
-    if (bytes)
-      asm volatile(
-          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
-              smem_u32(dst)),
-          "l"(xg), "r"(bytes), "r"(bar)
-          : "memory");
-    if (xin)  // the last entries when n * sizeof(T) is not a multiple of 16
-      for (int64_t i = bytes / sizeof(T); i < n; i++) dst[i] = __ldg(xg + i);
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
   };
-  auto wait_bar = [&](int slot, unsigned parity) -> bool {
-    const unsigned bar = smem_u32(&s_bar[slot]);
-    for (int i = 0; i < (1 << 22); i++) {
-      unsigned ok;
-      asm volatile(
-          "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-          : "=r"(ok)
-          : "r"(bar), "r"(parity)
-          : "memory");
-      if (ok) return true;
-    }
-    return false;
-  };
-
-  unsigned phase = 0;
   int cur = 0;
   fetch(0);
-  __syncthreads();
   while (true) {
     const int q = s_q[cur];
     if (q >= nitems) break;
-    fetch(cur ^ 1);
-    const bool ok = wait_bar(cur, (phase >> cur) & 1u);
-    phase ^= 1u << cur;
-    if (__syncthreads_or(!ok)) {  // a copy did not land: flag, drain (bounded), leave
-      if (threadIdx.x == 0) ws[3] = 2;
-      wait_bar(cur ^ 1, (phase >> (cur ^ 1)) & 1u);
-      return;
+    if constexpr (NBUF == 2) {
+      fetch(cur ^ 1);
+      asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+    } else {
+      asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     }
+    __syncthreads();  // x of matrix q is in shared memory
     const mgb_csr_batch_item it = items[__ldg(order + q)];
-    const T* xs = cur ? xbuf1 : xbuf0;
+    const T* xs = reinterpret_cast<const T*>(bat_smem + cur * BAT_XS_BYTES);
     const T* xg = static_cast<const T*>(it.x);
-    const bool xin = s_xin[cur] != 0;
-    int64_t chunk = (it.nnz + BAT_WARPS * CPW - 1) / (BAT_WARPS * CPW);
+    const bool xin = it.ncols <= XCAP;
+    int64_t chunk = (it.nnz + WARPS * CPW - 1) / (WARPS * CPW);
     chunk = chunk < 256 ? 256 : (chunk > 4096 ? 4096 : chunk);
     const int64_t nch = it.nnz / chunk + 1;
     const T* va = static_cast<const T*>(it.values);
     T* y = static_cast<T*>(it.y);
-    for (int64_t c = w; c < nch; c += BAT_WARPS) {
+    for (int64_t c = w; c < nch; c += WARPS) {
       if (xin)
         csr::csr_chunk_x<T, SEG>(c, chunk, it.nrows, it.ncols, it.row_offsets, it.column_indices, va,
                                  csr::XShared<T>{xs}, y, init, stage[w], lane);
@@ -204,8 +184,13 @@ spmv_batched_csr_xs(const mgb_csr_batch_item* __restrict__ items, int64_t nitems
                                  csr::XGlobal<T>{xg}, y, init, stage[w], lane);
     }
     __syncthreads();  // buffer `cur` and s_q[cur] are reused by the next fetch
-    cur ^= 1;
+    if constexpr (NBUF == 2) {
+      cur ^= 1;
+    } else {
+      fetch(0);
+    }
   }
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
 }
 
 // One CTA per matrix at a time with x read through L1 (configs >= BAT_FIRST_XL1):
@@ -310,17 +295,22 @@ int launch_cfg(const mgb_csr_batch_item* items, int64_t nitems, int32_t* ws, int
   if constexpr (CFG >= BAT_FIRST_XL1) {
     spmv_batched_csr_xl1<T, CFG><<<num_sms() * 3, BAT_WARPS * 32, 0, s>>>(items, nitems, ws, init);
   } else if constexpr (CFG >= BAT_FIRST_XS) {
-    constexpr size_t smem = 2 * BAT_XS_BYTES + BAT_WARPS * sizeof(csr::WarpStage<T, BAT_SEG[CFG]>);
+    // config 6: one x buffer, two CTAs of 8 warps per SM; config 7: two
+    // buffers (next matrix's x copied during this one), one CTA of 16 warps
+    constexpr int NBUF = CFG == BAT_FIRST_XS ? 1 : 2;
+    constexpr int WARPS = CFG == BAT_FIRST_XS ? 8 : 16;
+    constexpr size_t smem = NBUF * BAT_XS_BYTES + WARPS * sizeof(csr::WarpStage<T, BAT_SEG[CFG]>);
     // set once per device (a function attribute, not a stream operation)
     static std::atomic<bool> attr_set[64];
     int dev = 0;
     MGB_CUDA_CHECK(cudaGetDevice(&dev));
     if (dev < 0 || dev >= 64 || !attr_set[dev].load(std::memory_order_acquire)) {
-      MGB_CUDA_CHECK(cudaFuncSetAttribute(spmv_batched_csr_xs<T, CFG>,
+      MGB_CUDA_CHECK(cudaFuncSetAttribute(spmv_batched_csr_xs<T, CFG, NBUF, WARPS>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       if (dev >= 0 && dev < 64) attr_set[dev].store(true, std::memory_order_release);
     }
-    spmv_batched_csr_xs<T, CFG><<<num_sms() * 2, BAT_WARPS * 32, smem, s>>>(items, nitems, ws, init);
+    spmv_batched_csr_xs<T, CFG, NBUF, WARPS>
+        <<<num_sms() * (16 / WARPS), WARPS * 32, smem, s>>>(items, nitems, ws, init);
   } else {
     spmv_batched_csr<T, CFG><<<num_sms() * 3, BAT_WARPS * 32, 0, s>>>(items, nitems, ws, init);
   }

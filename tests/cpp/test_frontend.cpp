@@ -18,6 +18,7 @@
 // Build: g++ -std=c++17 -Iinclude -I<cuda>/include tests/cpp/test_frontend.cpp
 //        -Lmorpheus_gb300 -lmorpheus_gb300 -Loracle/_build -loracle -lcudart
 // Exit status 0 when every check passes; one line per failed check.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -239,6 +240,82 @@ void test_banded(int64_t n) {
     orc_convert(o.h, ob.h);
     expect(same_structure(back, ob), ft + " -> CSR: structure bit-exact with the Serial convert");
   }
+}
+
+// Irregular square CSR: row lengths 0..60 from a seeded generator (about a
+// fifth of the rows empty), distinct sorted columns, values U[-2, 2].
+template <class T>
+HostCsr<T> irregular(int64_t n, unsigned seed) {
+  HostCsr<T> h;
+  h.n = n;
+  std::mt19937_64 rng(seed);
+  std::uniform_int_distribution<int> L(0, 60);
+  std::uniform_int_distribution<int64_t> Cdist(0, n - 1);
+  std::uniform_real_distribution<double> U(-2.0, 2.0);
+  h.ro.push_back(0);
+  for (int64_t i = 0; i < n; i++) {
+    int len = L(rng);
+    len = len < 12 ? 0 : len;
+    std::vector<int32_t> cols;
+    for (int k = 0; k < len; k++) cols.push_back((int32_t)Cdist(rng));
+    std::sort(cols.begin(), cols.end());
+    cols.erase(std::unique(cols.begin(), cols.end()), cols.end());
+    for (int32_t c : cols) {
+      h.ci.push_back(c);
+      h.v.push_back((T)U(rng));
+    }
+    h.ro.push_back((int32_t)h.ci.size());
+  }
+  return h;
+}
+
+// The chunk plan cached by CsrMatrix: the planned multiply gives y bit for
+// bit equal to the unplanned lane-segment kernel, and writing new row
+// offsets through row_offsets() drops the plan (the next multiply matches
+// the Serial multiply of the new structure).
+template <class T>
+void test_chunk_plan() {
+  const int64_t n = 60000;
+  const std::string tag = std::string(tname<T>()) + " chunk plan";
+  const HostCsr<T> h = irregular<T>(n, 77);
+  Morpheus::CsrMatrix<T> A(n, n, h.ro, h.ci, h.v);
+  expect(A.kernel_variant() == MGB_CSR_SEGMENTS, tag + ": lane-segment kernel chosen");
+  const std::vector<T> xh = host_vector<T>(n, 5);
+  const Morpheus::DenseVector<T> x(xh);
+  Morpheus::DenseVector<T> y1(std::vector<T>((size_t)n, T(0))), y2(std::vector<T>((size_t)n, T(0)));
+  Morpheus::multiply<GB300>(A, x, y1);
+  const mgb_csr d = A.desc();
+  int st;
+  if constexpr (std::is_same_v<T, double>)
+    st = mgb_spmv_csr_variant_f64(&d, x.data(), y2.data(), 1, MGB_CSR_SEGMENTS, nullptr);
+  else
+    st = mgb_spmv_csr_variant_f32(&d, x.data(), y2.data(), 1, MGB_CSR_SEGMENTS, nullptr);
+  expect(st == MGB_SUCCESS, tag + ": unplanned call");
+  expect(same(y1.to_host(), y2.to_host()), tag + ": planned y bit-identical to the unplanned kernel");
+  int64_t entries = 0;
+  expect(A.chunk_plan(&entries) != nullptr && entries >= 2, tag + ": plan cached");
+
+  // same nnz, rows reversed: new row offsets written through the accessor
+  HostCsr<T> r;
+  r.n = n;
+  r.ro.push_back(0);
+  for (int64_t i = n - 1; i >= 0; i--) {
+    for (int32_t k = h.ro[i]; k < h.ro[i + 1]; k++) {
+      r.ci.push_back(h.ci[k]);
+      r.v.push_back(h.v[k]);
+    }
+    r.ro.push_back((int32_t)r.ci.size());
+  }
+  A.row_offsets().assign(r.ro);
+  A.column_indices().assign(r.ci);
+  A.values().assign(r.v);
+  Morpheus::multiply<GB300>(A, x, y1);
+  Oracle o(1, dtype_code<T>());
+  oracle_from_csr(o, r);
+  std::vector<T> ref((size_t)n, T(0));
+  orc_multiply(o.h, xh.data(), ref.data(), 1, 0);
+  const double e = rel_err(y1.to_host(), ref);
+  expect(e <= tol<T>(), tag + ": new row offsets after a cached plan, rel err " + std::to_string(e));
 }
 
 // in-place convert refused by the fill tolerance leaves the data in place
@@ -541,6 +618,8 @@ int main(int argc, char** argv) {
       test_banded<double>(n);
       test_banded<float>(n);
     }
+    test_chunk_plan<double>();
+    test_chunk_plan<float>();
     test_convert_errors();
     test_activate();
     test_sort();

@@ -93,6 +93,33 @@ def test_shared_x_configs_f32_and_wide_x(cuda, config):
         assert err <= 1e-5
 
 
+@pytest.mark.parametrize("config", [6, 7])
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_shared_x_configs_unaligned_x(cuda, config, dtype):
+    """x vectors that start one element past a 16-byte boundary are copied
+    into shared memory element by element; the result is unchanged."""
+    mats, dev, xs, ys, _ = make_batch(50, seed=40 + config, dtype=dtype)
+    xs = [torch.cat([torch.zeros(1, dtype=x.dtype, device=x.device), x])[1:] for x in xs]
+    assert all(x.data_ptr() % 16 != 0 for x in xs)
+    y0s = [y.cpu().numpy() for y in ys]
+    b = batched.CsrBatch(dev, xs, ys)
+    b.plan(config)
+    b.multiply(init=False)
+    torch.cuda.synchronize()
+    assert b.planned_ok()
+    for m, x, y, y0 in zip(mats, xs, ys, y0s):
+        m64 = dict(m, values=m["values"].astype(np.float64))
+        x64 = x.cpu().numpy().astype(np.float64)
+        ref = O.OracleMatrix.from_host(m64).multiply(x64, y0.astype(np.float64).copy(), init=False)
+        if dtype == np.float64:
+            assert rel_err(y.cpu().numpy(), ref) <= 1e-12
+        else:
+            scale = O.OracleMatrix.from_host(dict(m64, values=np.abs(m64["values"]))).multiply(
+                np.abs(x64), np.abs(y0.astype(np.float64)), init=False)
+            err = np.linalg.norm(y.double().cpu().numpy() - ref) / max(np.linalg.norm(scale), 1e-300)
+            assert err <= 1e-5
+
+
 def test_config_mismatch_is_a_noop(cuda):
     mats, dev, xs, ys, _ = make_batch(10, seed=5)
     b = batched.CsrBatch(dev, xs, ys)

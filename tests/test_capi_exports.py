@@ -80,3 +80,25 @@ def test_null_pointers_with_nonempty_sizes_rejected(lib_built):
     assert lib.mgb_spmv_dot_csr_f64(C.byref(d), None, None, 1, 1, None, None) == 8
     coo = _lib.Coo(10, 10, 5, None, None, None)
     assert lib.mgb_spmv_coo_f64(C.byref(coo), None, None, 1, None) == 8
+
+
+def test_chunk_plan_sizes_and_arguments_without_gpu(lib_built):
+    """The chunk plan has nnz / chunk + 2 entries (chunk 256..2048 nonzeros);
+    a missing plan, a plan of the wrong size, or a plan for another kernel is
+    refused before any device work."""
+    lib = _lib.load()
+    n = C.c_int64()
+    d = _lib.Csr(2_000_000, 2_000_000, 30_000_000, None, None, None)
+    assert lib.mgb_csr_plan_entries(C.byref(d), C.byref(n)) == 0
+    assert n.value == 30_000_000 // 2048 + 2
+    d0 = _lib.Csr(0, 0, 0, None, None, None)
+    assert lib.mgb_csr_plan_entries(C.byref(d0), C.byref(n)) == 0 and n.value == 2
+    bad = _lib.Csr(-1, 4, 0, None, None, None)
+    assert lib.mgb_csr_plan_entries(C.byref(bad), C.byref(n)) == 8
+    assert lib.mgb_csr_plan_entries(None, C.byref(n)) == 8
+    fake = C.c_void_p(256)  # never dereferenced: the size checks come first
+    df = _lib.Csr(2_000_000, 2_000_000, 30_000_000, fake, fake, fake)
+    assert lib.mgb_csr_plan(C.byref(df), None, n.value, None) == 8
+    assert lib.mgb_csr_plan(C.byref(df), fake, 10, None) == 8
+    assert lib.mgb_spmv_csr_planned_f64(C.byref(df), None, 10, fake, fake, 1, None) == 8
+    assert lib.mgb_spmv_csr_planned_f32(C.byref(df), fake, 10, fake, fake, 1, None) == 8

@@ -208,6 +208,86 @@ def test_csr_kernel_variants(cuda, variant, case, dtype):
         check(A, dtype, init, csr_variant=variant)
 
 
+def _unplanned_segments(A, x, y, init):
+    import ctypes as C
+    from morpheus_gb300 import _lib
+    sfx = "f64" if A.dtype == torch.float64 else "f32"
+    _lib.call(f"mgb_spmv_csr_variant_{sfx}", C.byref(A._desc()), C.c_void_p(x.data_ptr()),
+              C.c_void_p(y.data_ptr()), 1 if init else 0, mgb.CSR_SEGMENTS, None)
+
+
+def _segments_chunk(nrows, nnz):
+    """The lane-segment kernel's chunk size rule (2048, halved down to 256
+    while the matrix gives fewer chunks than resident warps and a chunk
+    spans >= 8 mean rows)."""
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    chunk, mean = 2048, nnz // max(nrows, 1)
+    while chunk > 256 and nnz // chunk < sms * 24 and chunk // 2 >= 8 * mean:
+        chunk >>= 1
+    return chunk
+
+
+@pytest.mark.parametrize("case", ["stencil27", "laplacian", "banded", "power_law", "empty_rows",
+                                  "long_rows", "ragged_tail", "huge_row", "all_empty_tail",
+                                  "all_empty", "tiny", "no_rows"])
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_chunk_plan_bit_identical(cuda, case, dtype):
+    """The chunk plan holds the lower bounds of k*chunk in row_offsets, and
+    the planned multiply (what multiply() runs for the lane-segment kernel)
+    gives y bit for bit equal to the kernel's own row search."""
+    if case == "all_empty":
+        hm = gen.random_lengths_csr(300, 300, np.zeros(300, dtype=np.int64), seed=3, dtype=dtype)
+    elif case == "tiny":
+        hm = gen.random_lengths_csr(3, 3, np.array([1, 0, 2]), seed=10, dtype=dtype)
+    elif case == "no_rows":
+        hm = gen.random_lengths_csr(0, 5, np.zeros(0, dtype=np.int64), seed=4, dtype=dtype)
+    else:
+        hm = _csr_case(case, dtype)
+    A = mgb.matrix_from_host(hm, device="cuda")
+    A._variant = mgb.CSR_SEGMENTS
+    plan, entries = A.chunk_plan()
+    torch.cuda.synchronize()
+    ro = hm["row_offsets"].astype(np.int64)
+    chunk = _segments_chunk(hm["nrows"], hm["nnz"])
+    assert entries == hm["nnz"] // chunk + 2
+    want = np.minimum(np.searchsorted(ro, np.arange(entries, dtype=np.int64) * chunk, side="left"), hm["nrows"])
+    assert np.array_equal(plan.cpu().numpy(), want)
+    x = torch.from_numpy(gen.x_vector(hm["ncols"], seed=5, dtype=dtype)).cuda()
+    for init in (True, False):
+        y0 = torch.from_numpy(gen.x_vector(hm["nrows"], seed=6, dtype=dtype)).cuda()
+        y1, y2 = y0.clone(), y0.clone()
+        mgb.multiply(A, x, y1, init=init)
+        _unplanned_segments(A, x, y2, init)
+        torch.cuda.synchronize()
+        assert torch.equal(y1, y2)
+        if hm["nrows"]:
+            om = O.OracleMatrix.from_host(hm)
+            ref = om.multiply(x.cpu().numpy(), y0.cpu().numpy().copy(), init=init)
+            assert rel_err(y1.cpu().numpy(), ref) <= TOL[dtype]
+
+
+def test_chunk_plan_dropped_with_kernel_choice(cuda):
+    """After new row offsets are written in place, forget_kernel_variant()
+    drops the cached plan and the next multiply uses the new structure."""
+    lens = np.zeros(20000, dtype=np.int64)
+    lens[::2] = 30
+    hm = gen.random_lengths_csr(20000, 20000, lens, seed=31)
+    A = mgb.matrix_from_host(hm, device="cuda")
+    x = torch.from_numpy(gen.x_vector(20000, seed=2)).cuda()
+    y = torch.zeros(20000, dtype=torch.float64, device="cuda")
+    A._variant = mgb.CSR_SEGMENTS
+    mgb.multiply(A, x, y)
+    # the same entries, rows shifted by one: odd rows hold them now
+    hm2 = dict(hm, row_offsets=np.concatenate([[0], hm["row_offsets"][:-1]]).astype(np.int32))
+    A.row_offsets().copy_(torch.from_numpy(hm2["row_offsets"]).cuda())
+    A.forget_kernel_variant()
+    A._variant = mgb.CSR_SEGMENTS
+    mgb.multiply(A, x, y)
+    torch.cuda.synchronize()
+    ref = O.OracleMatrix.from_host(hm2).multiply(x.cpu().numpy())
+    assert rel_err(y.cpu().numpy(), ref) <= 1e-12
+
+
 @pytest.mark.parametrize("case,expect", [("stencil27", "rows"), ("laplacian", "rows"), ("banded", "rows"),
                                          ("power_law", "segments"), ("long_rows", "split"),
                                          ("empty_rows", "segments"), ("huge_row", "split")])
