@@ -8,7 +8,7 @@ from .algorithms import dot, dot_async, multiply, multiply_host, reduce, waxpby
 from .batched import CsrBatch
 from .convert import convert, convert_inplace, from_coo, is_sorted, sort_by_row_and_column, to_coo
 from .containers import (COO_FORMAT, CSR_FORMAT, DIA_FORMAT, ELL_FORMAT, HDC_FORMAT, HYB_FORMAT,
-                         CSR_ROWS, CSR_SEGMENTS, CSR_SPLIT, INVALID_INDEX, NFORMATS, CooMatrix, CsrMatrix, DiaMatrix, DynamicMatrix,
+                         CSR_ROWS, CSR_ROWS_GATHER, CSR_SEGMENTS, CSR_SPLIT, INVALID_INDEX, NFORMATS, CooMatrix, CsrMatrix, DiaMatrix, DynamicMatrix,
                          EllMatrix, HdcMatrix, HybMatrix, conversion_error_e, formats_e, get_pad_size,
                          matrix_from_host, matrix_to_host)
 from .matrix_market import read_matrix_market_file, write_matrix_market_file
@@ -23,7 +23,7 @@ __all__ = [
     "CooMatrix", "CsrMatrix", "DiaMatrix", "EllMatrix", "HybMatrix", "HdcMatrix", "DynamicMatrix",
     "formats_e", "conversion_error_e", "get_pad_size", "matrix_from_host", "matrix_to_host",
     "COO_FORMAT", "CSR_FORMAT", "DIA_FORMAT", "ELL_FORMAT", "HYB_FORMAT", "HDC_FORMAT", "NFORMATS",
-    "INVALID_INDEX", "CSR_SEGMENTS", "CSR_ROWS", "CSR_SPLIT",
+    "INVALID_INDEX", "CSR_SEGMENTS", "CSR_ROWS", "CSR_SPLIT", "CSR_ROWS_GATHER",
     "read_matrix_market_file", "write_matrix_market_file",
     "MorpheusException", "NotImplementedException", "FormatConversionException",
     "InvalidInputException", "RuntimeException", "IOException", "CudaException",

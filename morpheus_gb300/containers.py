@@ -44,8 +44,9 @@ class conversion_error_e(enum.IntEnum):
 
 COO_FORMAT, CSR_FORMAT, DIA_FORMAT, ELL_FORMAT, HYB_FORMAT, HDC_FORMAT, NFORMATS = range(7)
 INVALID_INDEX = -1
-# CSR SpMV kernels (MGB_CSR_SEGMENTS / MGB_CSR_ROWS / MGB_CSR_SPLIT of include/mgb.h)
-CSR_SEGMENTS, CSR_ROWS, CSR_SPLIT = 1, 2, 3
+# CSR SpMV kernels (MGB_CSR_SEGMENTS / MGB_CSR_ROWS / MGB_CSR_SPLIT /
+# MGB_CSR_ROWS_GATHER of include/mgb.h)
+CSR_SEGMENTS, CSR_ROWS, CSR_SPLIT, CSR_ROWS_GATHER = 1, 2, 3, 4
 
 
 def get_pad_size(length: int, alignment: int) -> int:
@@ -163,8 +164,9 @@ class CsrMatrix(_Matrix):
     cvalues = values
 
     def kernel_variant(self) -> int:
-        """SpMV kernel for this matrix (CSR_ROWS for short rows of nearly
-        equal length, else CSR_SEGMENTS), measured once on the device and
+        """SpMV kernel for this matrix (CSR_ROWS / CSR_ROWS_GATHER for short
+        rows of nearly equal length with neighbouring / scattered columns,
+        CSR_SPLIT for very long rows, else CSR_SEGMENTS), measured once on the device and
         cached.  Values may change in place; after writing new row offsets in
         place, call forget_kernel_variant()."""
         if self._variant is None:

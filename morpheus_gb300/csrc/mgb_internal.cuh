@@ -59,7 +59,7 @@ int launch_ell(const mgb_ell* A, const T* x, T* y, int init, cudaStream_t s);
 template <typename T>
 int launch_coo(const mgb_coo* A, const T* x, T* y, int init, cudaStream_t s);
 // CSR SpMV with an explicit kernel (MGB_CSR_SEGMENTS / MGB_CSR_ROWS /
-// MGB_CSR_SPLIT).  With partials != nullptr the kernel also forms
+// MGB_CSR_SPLIT / MGB_CSR_ROWS_GATHER).  With partials != nullptr the kernel also forms
 // x[0..nrows) . y, one partial per warp, *npartials of them; partials ==
 // nullptr with npartials != nullptr only reports that count.  plan: an
 // optional chunk plan of plan_entries entries (lane-segment kernel only).
@@ -68,9 +68,12 @@ int launch_csr_dot(const mgb_csr* A, const T* x, T* y, int init, void* stream, i
                    int64_t* npartials, const int32_t* plan = nullptr, int64_t plan_entries = 0);
 template <typename T>
 int launch_csr_rows(const mgb_csr* A, const T* x, T* y, int init, cudaStream_t s, T* partials = nullptr,
-                    int64_t* npartials = nullptr);
+                    int64_t* npartials = nullptr, bool gather = false);
 
 // Validation helpers for descriptors.
 inline bool bad_sizes(int64_t a, int64_t b, int64_t c) { return a < 0 || b < 0 || c < 0; }
+inline bool valid_csr_variant(int v) {
+  return v == MGB_CSR_SEGMENTS || v == MGB_CSR_ROWS || v == MGB_CSR_SPLIT || v == MGB_CSR_ROWS_GATHER;
+}
 
 }  // namespace mgb

@@ -210,7 +210,7 @@ __global__ void __launch_bounds__(FIN_THREADS) cg_init_state(const T* __restrict
 template <typename T>
 int check_csr(const mgb_csr* A, int variant) {
   MGB_REQUIRE(A != nullptr && !bad_sizes(A->nrows, A->ncols, A->nnz), MGB_ERR_BAD_ARGUMENT);
-  MGB_REQUIRE(variant == MGB_CSR_SEGMENTS || variant == MGB_CSR_ROWS || variant == MGB_CSR_SPLIT,
+  MGB_REQUIRE(valid_csr_variant(variant),
               MGB_ERR_BAD_ARGUMENT);
   return MGB_SUCCESS;
 }

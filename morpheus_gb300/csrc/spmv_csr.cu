@@ -217,13 +217,14 @@ int launch_csr_dot(const mgb_csr* A, const T* x, T* y, int init, void* stream, i
   MGB_REQUIRE(A != nullptr, MGB_ERR_BAD_ARGUMENT);
   MGB_REQUIRE(!bad_sizes(A->nrows, A->ncols, A->nnz), MGB_ERR_BAD_ARGUMENT);
   MGB_REQUIRE(A->nnz < ((int64_t)1 << 31) - 4096, MGB_ERR_INVALID_INPUT);
-  MGB_REQUIRE(variant == MGB_CSR_SEGMENTS || variant == MGB_CSR_ROWS || variant == MGB_CSR_SPLIT,
+  MGB_REQUIRE(valid_csr_variant(variant),
               MGB_ERR_BAD_ARGUMENT);
   if (A->nrows == 0) return MGB_SUCCESS;
   MGB_REQUIRE(A->row_offsets != nullptr && y != nullptr, MGB_ERR_BAD_ARGUMENT);
   MGB_REQUIRE(A->nnz == 0 || (A->column_indices && A->values && x), MGB_ERR_BAD_ARGUMENT);
   MGB_REQUIRE(plan == nullptr || variant == MGB_CSR_SEGMENTS, MGB_ERR_BAD_ARGUMENT);
-  if (variant == MGB_CSR_ROWS) return launch_csr_rows<T>(A, x, y, init, as_stream(stream), partials, npartials);
+  if (variant == MGB_CSR_ROWS || variant == MGB_CSR_ROWS_GATHER)
+    return launch_csr_rows<T>(A, x, y, init, as_stream(stream), partials, npartials, variant == MGB_CSR_ROWS_GATHER);
   if (variant == MGB_CSR_SPLIT) return launch_split<T>(A, x, y, init, as_stream(stream), partials, npartials);
   const int64_t chunk = segments_chunk(A);
   const int64_t nchunks = A->nnz / chunk + 1;

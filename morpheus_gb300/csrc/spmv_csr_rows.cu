@@ -1,42 +1,84 @@
 // spmv_csr_rows.cu -- CSR SpMV for rows of (nearly) equal, short length, and
-// the per-matrix choice between the two CSR kernels.
+// the per-matrix choice between the CSR kernels.
 //
 // The reference chooses its scalar (thread-per-row) CSR kernel only when the
 // user sets MATOPT_SHORT_ROWS (impl/Csr/Cuda/Morpheus_Multiply_Impl.hpp:59-92).
 // Here the choice is measured: mgb_csr_choose_kernel reads the row lengths
-// once and picks
-//   MGB_CSR_ROWS     when 32 rows of the longest length fit one staged tile
-//                    (longest row <= 28) and the longest row is <= 1.5 x
-//                    mean + 2 (stencils, banded matrices, FEM meshes), else
-//   MGB_CSR_SPLIT    when some row is longer than 8192 entries or rows
-//                    average >= 512 (split nonzero chunks with carries,
-//                    spmv_csr.cu), else
-//   MGB_CSR_SEGMENTS the lane-segment kernel of spmv_csr.cu (any structure).
+// and the columns of a sample of neighbouring rows once and picks
+//   MGB_CSR_SPLIT       when some row is longer than 8192 entries or rows
+//                       average >= 512 (split nonzero chunks with carries,
+//                       spmv_csr.cu), else, for short rows of nearly equal
+//                       length (longest row <= 28 and <= 1.5 x mean + 2):
+//   MGB_CSR_ROWS        when neighbouring rows read neighbouring columns
+//                       (stencils, banded matrices, FEM meshes), or
+//   MGB_CSR_ROWS_GATHER when their columns are scattered and rows are at
+//                       most 20 long, else
+//   MGB_CSR_SEGMENTS    the lane-segment kernel of spmv_csr.cu (any structure).
 //
 // Row-tile kernel: one warp owns 32 consecutive rows.  The tile's entries are
-// one contiguous range of the CSR arrays; up to ROWS_TILE_MAX of them are
-// staged into shared memory with coalesced loads, then every lane walks its
-// own row from shared memory in lockstep with the others (equal lengths keep
-// every FP64 FMA full-warp), and neighbouring rows read neighbouring x
-// entries, so the x loads of a warp are (nearly) coalesced instead of 32
-// separate gathers.  Tiles whose range is longer are processed in pieces.
+// one contiguous range of the CSR arrays; up to TILE of them at a time are
+// staged into shared memory with cp.async (all in flight at once), then every
+// lane walks its own row from shared memory in lockstep with the others
+// (equal lengths keep every FP64 FMA full-warp), issuing its x reads 8, 4,
+// 2, 1 at a time so that FMA slots match the row length exactly.  The staging
+// size is a trade measured on GB300:
+//   * MGB_CSR_ROWS sizes TILE to hold a whole tile (32 x mean row length):
+//     224 / 448 / 896 entries with 12 / 10 / 5 CTAs of 4 warps per SM.  With
+//     neighbouring rows reading neighbouring x entries, a warp's x reads
+//     touch few sectors and more resident warps win (5-point Laplacian
+//     125 -> 69 us, 13-point band 96 -> 78 us).
+//   * MGB_CSR_ROWS_GATHER stages 224 entries at a time with 10 CTAs per SM,
+//     leaving about 140 KB of the SM's 256 KB for L1: scattered x reads need
+//     L1 lines to be in flight, and with 215 KB of shared memory the same
+//     kernel ran 2x slower (12 random entries per row: 213 -> 109 us, the
+//     lane-segment kernel 146 us).
+#include "mgb_internal.cuh"
 #include "mgb_internal.cuh"
 
 namespace mgb {
 namespace {
 
 constexpr int ROWS_WARPS = 4;
-constexpr int ROWS_TILE_MAX = 896;  // 32 rows x 28 entries
+constexpr int ROWS_TILE_MAX = 896;  // 32 rows x 28 entries: the longest rows a tile is chosen for
+constexpr int ROWS_GATHER_MAX = 20;  // longest scattered rows MGB_CSR_ROWS_GATHER is chosen for
+
+__device__ __forceinline__ unsigned rows_smem_u32(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+// one element global -> shared with cp.async (no register round trip)
+template <int BYTES>
+__device__ __forceinline__ void cp_async_elem(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(rows_smem_u32(dst)), "l"(src), "n"(BYTES)
+               : "memory");
+}
+
+// x reads of U consecutive entries of every lane's row, then their FMAs
+template <int U, typename T>
+__device__ __forceinline__ void rows_step(int32_t j, int32_t lo, int32_t hi, int32_t c, int64_t ncols,
+                                          const T* sv, const int32_t* sc, const T* __restrict__ x, T& acc) {
+  T xv[U], vv[U];
+#pragma unroll
+  for (int q = 0; q < U; q++) {
+    const int32_t e = lo + j + q;
+    const bool ok = e < hi;
+    const int32_t col = ok ? sc[e - c] : 0;
+    vv[q] = ok ? sv[e - c] : T(0);
+    xv[q] = (ok && (unsigned)col < (uint64_t)ncols) ? __ldg(x + col) : T(0);
+  }
+#pragma unroll
+  for (int q = 0; q < U; q++)
+    if (lo + j + q < hi) acc = fmadd(vv[q], xv[q], acc);
+}
 
 // DOT: also x[0..nrows) . y, one partial per warp in
 // partials[blockIdx.x * ROWS_WARPS + warp].
-template <typename T, bool DOT>
-__global__ void __launch_bounds__(ROWS_WARPS * 32, 5)
+template <typename T, bool DOT, int TILE, int MINB>
+__global__ void __launch_bounds__(ROWS_WARPS * 32, MINB)
 spmv_csr_rowtile(int64_t nrows, int64_t ncols, const int32_t* __restrict__ ro, const int32_t* __restrict__ ci,
                  const T* __restrict__ va, const T* __restrict__ x, T* __restrict__ y, int init,
                  T* __restrict__ partials) {
-  __shared__ T s_val[ROWS_WARPS][ROWS_TILE_MAX];
-  __shared__ int32_t s_col[ROWS_WARPS][ROWS_TILE_MAX];
+  __shared__ T s_val[ROWS_WARPS][TILE];
+  __shared__ int32_t s_col[ROWS_WARPS][TILE];
   const int lane = threadIdx.x & 31;
   const int w = threadIdx.x >> 5;
   T* sv = s_val[w];
@@ -52,26 +94,29 @@ spmv_csr_rowtile(int64_t nrows, int64_t ncols, const int32_t* __restrict__ ro, c
     const int32_t tb = __shfl_sync(0xffffffffu, rs, 0);
     const int32_t te = (int32_t)__reduce_max_sync(0xffffffffu, (unsigned)re);
     T acc = (valid && !init) ? y[r] : T(0);
-    for (int32_t c = tb; c < te; c += ROWS_TILE_MAX) {
-      const int32_t cend = (te - c < ROWS_TILE_MAX) ? te : c + ROWS_TILE_MAX;
-      __syncwarp();
+    for (int32_t c = tb; c < te; c += TILE) {
+      const int32_t cend = (te - c < TILE) ? te : c + TILE;
+      __syncwarp();  // the previous piece's shared-memory reads are done
       for (int32_t i = c + lane; i < cend; i += 32) {
-        sv[i - c] = ldg_stream(va + i);
-        sc[i - c] = ldg_stream(ci + i);
+        cp_async_elem<sizeof(T)>(sv + (i - c), va + i);
+        cp_async_elem<4>(sc + (i - c), ci + i);
       }
+      asm volatile("cp.async.wait_all;\n" ::: "memory");
       __syncwarp();
       const int32_t lo = max(rs, c), hi = min(re, cend);
-      // lockstep over the longest intersection in the warp
+      // lockstep over the longest intersection in the warp (n is warp-uniform)
       const int32_t n = (int32_t)__reduce_max_sync(0xffffffffu, (unsigned)max(hi - lo, 0));
-#pragma unroll 4
-      for (int32_t j = 0; j < n; j++) {
-        const int32_t e = lo + j;
-        if (e < hi) {
-          const int32_t col = sc[e - c];
-          const T xv = ((unsigned)col < (uint64_t)ncols) ? __ldg(x + col) : T(0);
-          acc = fmadd(sv[e - c], xv, acc);
-        }
+      int32_t j = 0;
+      for (; j + 8 <= n; j += 8) rows_step<8>(j, lo, hi, c, ncols, sv, sc, x, acc);
+      if (j + 4 <= n) {
+        rows_step<4>(j, lo, hi, c, ncols, sv, sc, x, acc);
+        j += 4;
       }
+      if (j + 2 <= n) {
+        rows_step<2>(j, lo, hi, c, ncols, sv, sc, x, acc);
+        j += 2;
+      }
+      if (j < n) rows_step<1>(j, lo, hi, c, ncols, sv, sc, x, acc);
     }
     if (valid) {
       y[r] = acc;
@@ -84,29 +129,76 @@ spmv_csr_rowtile(int64_t nrows, int64_t ncols, const int32_t* __restrict__ ro, c
   }
 }
 
-__global__ void row_shape_kernel(const int32_t* __restrict__ ro, int64_t nrows, int* mx) {
+// Row shape of a CSR matrix: shape[0] = longest row; over every 16th row r
+// (and row r + 1), shape[1] = entries k of the shorter of the two rows with
+// |col(r+1, k) - col(r, k) - 1| <= 2 (neighbouring rows reading neighbouring
+// columns), shape[2] = entries compared.
+__global__ void row_shape_kernel(const int32_t* __restrict__ ro, const int32_t* __restrict__ ci, int64_t nrows,
+                                 unsigned long long* shape) {
   int m = 0;
-  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += (int64_t)gridDim.x * blockDim.x)
-    m = max(m, ro[r + 1] - ro[r]);
+  unsigned long long near = 0, cmp = 0;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t a = ro[r], b = ro[r + 1];
+    m = max(m, b - a);
+    if ((r & 15) == 0 && r + 1 < nrows) {
+      const int32_t b2 = ro[r + 2];
+      const int32_t len = min(min(b - a, b2 - b), 64);
+      for (int32_t k = 0; k < len; k++) {
+        const int64_t d = (int64_t)ci[b + k] - (int64_t)ci[a + k] - 1;
+        near += (d >= -2 && d <= 2) ? 1u : 0u;
+      }
+      cmp += (unsigned long long)(len > 0 ? len : 0);
+    }
+  }
   m = __reduce_max_sync(0xffffffffu, m);
-  if ((threadIdx.x & 31) == 0) atomicMax(mx, m);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    near += __shfl_xor_sync(0xffffffffu, near, o);
+    cmp += __shfl_xor_sync(0xffffffffu, cmp, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(shape, (unsigned long long)m);
+    atomicAdd(shape + 1, near);
+    atomicAdd(shape + 2, cmp);
+  }
+}
+
+// staging size of MGB_CSR_ROWS: the smallest of 224 / 448 / 896 entries that
+// holds a tile of 32 rows of the mean length (tiles longer than TILE are
+// processed in pieces, so this is a performance choice only)
+template <typename T, bool DOT, int TILE, int MINB>
+void launch_rows_cfg(const mgb_csr* A, const T* x, T* y, int init, cudaStream_t s, T* partials, unsigned blocks) {
+  spmv_csr_rowtile<T, DOT, TILE, MINB><<<blocks, ROWS_WARPS * 32, 0, s>>>(
+      A->nrows, A->ncols, A->row_offsets, A->column_indices, static_cast<const T*>(A->values), x, y, init,
+      partials);
+}
+
+template <typename T, bool DOT>
+void launch_rows_variant(const mgb_csr* A, const T* x, T* y, int init, cudaStream_t s, T* partials,
+                         unsigned blocks, bool gather) {
+  const int64_t tile_entries = 32 * (A->nnz / (A->nrows > 0 ? A->nrows : 1)) + 8;
+  if (gather)
+    launch_rows_cfg<T, DOT, 224, 10>(A, x, y, init, s, partials, blocks);
+  else if (tile_entries <= 224)
+    launch_rows_cfg<T, DOT, 224, 12>(A, x, y, init, s, partials, blocks);
+  else if (tile_entries <= 448)
+    launch_rows_cfg<T, DOT, 448, 10>(A, x, y, init, s, partials, blocks);
+  else
+    launch_rows_cfg<T, DOT, 896, 5>(A, x, y, init, s, partials, blocks);
 }
 
 template <typename T>
-int launch_rows(const mgb_csr* A, const T* x, T* y, int init, cudaStream_t s, T* partials, int64_t* npartials) {
+int launch_rows(const mgb_csr* A, const T* x, T* y, int init, cudaStream_t s, T* partials, int64_t* npartials,
+                bool gather) {
   const int64_t ntiles = (A->nrows + 31) / 32;
   int64_t blocks = (ntiles + ROWS_WARPS - 1) / ROWS_WARPS;
   if (blocks > 0x7fffffffLL) blocks = 0x7fffffffLL;
   if (npartials) *npartials = blocks * ROWS_WARPS;
   if (npartials && !partials) return MGB_SUCCESS;
   if (partials)
-    spmv_csr_rowtile<T, true><<<(unsigned)blocks, ROWS_WARPS * 32, 0, s>>>(
-        A->nrows, A->ncols, A->row_offsets, A->column_indices, static_cast<const T*>(A->values), x, y, init,
-        partials);
+    launch_rows_variant<T, true>(A, x, y, init, s, partials, (unsigned)blocks, gather);
   else
-    spmv_csr_rowtile<T, false><<<(unsigned)blocks, ROWS_WARPS * 32, 0, s>>>(
-        A->nrows, A->ncols, A->row_offsets, A->column_indices, static_cast<const T*>(A->values), x, y, init,
-        nullptr);
+    launch_rows_variant<T, false>(A, x, y, init, s, nullptr, (unsigned)blocks, gather);
   MGB_LAUNCH_CHECK();
   return MGB_SUCCESS;
 }
@@ -116,24 +208,29 @@ int choose(const mgb_csr* A, int* variant, cudaStream_t s) {
   MGB_REQUIRE(!bad_sizes(A->nrows, A->ncols, A->nnz), MGB_ERR_BAD_ARGUMENT);
   *variant = MGB_CSR_SEGMENTS;
   if (A->nrows == 0 || A->nnz == 0) return MGB_SUCCESS;
-  MGB_REQUIRE(A->row_offsets != nullptr, MGB_ERR_BAD_ARGUMENT);
-  int* d = nullptr;
-  MGB_CUDA_CHECK(cudaMallocAsync((void**)&d, sizeof(int), s));
-  cudaError_t e = cudaMemsetAsync(d, 0, sizeof(int), s);
+  MGB_REQUIRE(A->row_offsets != nullptr && A->column_indices != nullptr, MGB_ERR_BAD_ARGUMENT);
+  unsigned long long* d = nullptr;
+  MGB_CUDA_CHECK(cudaMallocAsync((void**)&d, 3 * sizeof(unsigned long long), s));
+  cudaError_t e = cudaMemsetAsync(d, 0, 3 * sizeof(unsigned long long), s);
   if (e == cudaSuccess) {
     int64_t blocks = (A->nrows + 255) / 256;
     const int64_t cap = (int64_t)num_sms() * 8;
     if (blocks > cap) blocks = cap;
-    row_shape_kernel<<<(unsigned)blocks, 256, 0, s>>>(A->row_offsets, A->nrows, d);
+    row_shape_kernel<<<(unsigned)blocks, 256, 0, s>>>(A->row_offsets, A->column_indices, A->nrows, d);
     e = cudaGetLastError();
   }
-  int mx = 0;
-  if (e == cudaSuccess) e = cudaMemcpyAsync(&mx, d, sizeof(int), cudaMemcpyDeviceToHost, s);
+  unsigned long long shape[3] = {0, 0, 0};
+  if (e == cudaSuccess) e = cudaMemcpyAsync(shape, d, sizeof(shape), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   cudaFreeAsync(d, s);
   if (e != cudaSuccess) return record_cuda_error(e);
+  const double mx = (double)shape[0];
   const double mean = (double)A->nnz / (double)A->nrows;
-  if (32 * mx <= ROWS_TILE_MAX && (double)mx <= 1.5 * mean + 2.0) *variant = MGB_CSR_ROWS;
+  const bool neighbouring = shape[2] == 0 || 2 * shape[1] >= shape[2];
+  if (32 * mx <= ROWS_TILE_MAX && mx <= 1.5 * mean + 2.0) {
+    if (neighbouring) *variant = MGB_CSR_ROWS;
+    else if (mx <= ROWS_GATHER_MAX) *variant = MGB_CSR_ROWS_GATHER;
+  }
   // rows longer than a few chunks: one warp per row would be the critical
   // path (measured: a 150,000-entry row 746 -> 56 us; rows of 1,000-6,000
   // entries 66 -> 46 us; the power-law matrix, mean 15, stays faster whole)
@@ -145,11 +242,14 @@ int choose(const mgb_csr* A, int* variant, cudaStream_t s) {
 
 // CSR SpMV entry with an explicit kernel choice (used by spmv_csr.cu too)
 template <typename T>
-int launch_csr_rows(const mgb_csr* A, const T* x, T* y, int init, cudaStream_t s, T* partials, int64_t* npartials) {
-  return launch_rows<T>(A, x, y, init, s, partials, npartials);
+int launch_csr_rows(const mgb_csr* A, const T* x, T* y, int init, cudaStream_t s, T* partials, int64_t* npartials,
+                    bool gather) {
+  return launch_rows<T>(A, x, y, init, s, partials, npartials, gather);
 }
-template int launch_csr_rows<double>(const mgb_csr*, const double*, double*, int, cudaStream_t, double*, int64_t*);
-template int launch_csr_rows<float>(const mgb_csr*, const float*, float*, int, cudaStream_t, float*, int64_t*);
+template int launch_csr_rows<double>(const mgb_csr*, const double*, double*, int, cudaStream_t, double*, int64_t*,
+                                     bool);
+template int launch_csr_rows<float>(const mgb_csr*, const float*, float*, int, cudaStream_t, float*, int64_t*,
+                                    bool);
 
 }  // namespace mgb
 

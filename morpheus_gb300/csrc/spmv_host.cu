@@ -79,7 +79,7 @@ template <typename T>
 int spmv_csr_host(const mgb_csr* A, const T* xh, T* yh, int init, int variant, int64_t nblocks, void* workspace,
                   int64_t workspace_bytes, cudaStream_t s) {
   MGB_REQUIRE(A != nullptr && !bad_sizes(A->nrows, A->ncols, A->nnz), MGB_ERR_BAD_ARGUMENT);
-  MGB_REQUIRE(variant == MGB_CSR_SEGMENTS || variant == MGB_CSR_ROWS || variant == MGB_CSR_SPLIT,
+  MGB_REQUIRE(valid_csr_variant(variant),
               MGB_ERR_BAD_ARGUMENT);
   MGB_REQUIRE(A->nnz < ((int64_t)1 << 31) - 4096, MGB_ERR_INVALID_INPUT);
   const int64_t N = A->nrows, M = A->ncols, nnz = A->nnz;

@@ -62,7 +62,7 @@ def test_host_spmv_matches_oracle(cuda, case, dtype, nblocks):
         _check(hm, dtype, init, nblocks, pin=True)
 
 
-@pytest.mark.parametrize("variant", [mgb.CSR_SEGMENTS, mgb.CSR_ROWS, mgb.CSR_SPLIT])
+@pytest.mark.parametrize("variant", [mgb.CSR_SEGMENTS, mgb.CSR_ROWS, mgb.CSR_SPLIT, mgb.CSR_ROWS_GATHER])
 def test_host_spmv_every_kernel_and_pageable(cuda, variant):
     hm = gen.power_law(20000, seed=56)
     _check(hm, np.float64, True, 4, pin=False, variant=variant)

@@ -40,7 +40,7 @@ def big(cuda):
     del A, ci, va
 
 
-@pytest.mark.parametrize("variant", [mgb.CSR_SEGMENTS, mgb.CSR_ROWS, mgb.CSR_SPLIT])
+@pytest.mark.parametrize("variant", [mgb.CSR_SEGMENTS, mgb.CSR_ROWS, mgb.CSR_SPLIT, mgb.CSR_ROWS_GATHER])
 def test_csr_at_int32_limit(big, variant):
     A, x, y_ref = big
     A._variant = variant

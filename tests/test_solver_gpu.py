@@ -48,7 +48,7 @@ CASES = {
 
 
 @pytest.mark.parametrize("case", list(CASES))
-@pytest.mark.parametrize("variant", [mgb.CSR_SEGMENTS, mgb.CSR_ROWS, mgb.CSR_SPLIT])
+@pytest.mark.parametrize("variant", [mgb.CSR_SEGMENTS, mgb.CSR_ROWS, mgb.CSR_SPLIT, mgb.CSR_ROWS_GATHER])
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
 def test_multiply_dot(cuda, case, variant, dtype):
     hm = CASES[case](dtype)
@@ -97,7 +97,7 @@ def test_waxpby_dot(cuda, n):
     assert abs(d.item() - float(wr @ wr)) <= 1e-13 * float(wr @ wr)
 
 
-@pytest.mark.parametrize("variant", [mgb.CSR_SEGMENTS, mgb.CSR_ROWS, mgb.CSR_SPLIT])
+@pytest.mark.parametrize("variant", [mgb.CSR_SEGMENTS, mgb.CSR_ROWS, mgb.CSR_SPLIT, mgb.CSR_ROWS_GATHER])
 def test_cg_follows_the_recurrence(cuda, variant):
     """25 iterations (rtol 0): the device iterate equals the FP64 restatement
     to rounding (CG amplifies rounding differences slowly on a

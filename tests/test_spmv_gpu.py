@@ -189,6 +189,10 @@ def _csr_case(case, dtype):
         lens[1500] = 150000
         lens[1501] = 2047
         return gen.random_lengths_csr(4000, 200000, lens, seed=27, dtype=dtype)
+    if case == "scattered12":  # 12 entries per row, uniform random columns
+        return gen.random_lengths_csr(20000, 20000, np.full(20000, 12), seed=29, dtype=dtype)
+    if case == "scattered24":  # 24 entries per row, uniform random columns
+        return gen.random_lengths_csr(20000, 20000, np.full(20000, 24), seed=30, dtype=dtype)
     if case == "all_empty_tail":  # entries only in the first rows, long empty tail
         lens = np.zeros(10000, dtype=np.int64)
         lens[:50] = 4096
@@ -196,9 +200,9 @@ def _csr_case(case, dtype):
     raise ValueError(case)
 
 
-@pytest.mark.parametrize("variant", [mgb.CSR_SEGMENTS, mgb.CSR_ROWS, mgb.CSR_SPLIT])
+@pytest.mark.parametrize("variant", [mgb.CSR_SEGMENTS, mgb.CSR_ROWS, mgb.CSR_SPLIT, mgb.CSR_ROWS_GATHER])
 @pytest.mark.parametrize("case", ["stencil27", "laplacian", "banded", "power_law", "empty_rows",
-                                  "long_rows", "ragged_tail", "huge_row", "all_empty_tail"])
+                                  "long_rows", "ragged_tail", "huge_row", "all_empty_tail", "scattered12"])
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
 def test_csr_kernel_variants(cuda, variant, case, dtype):
     """Both CSR kernels give the Serial result on every structure, whichever
@@ -290,10 +294,12 @@ def test_chunk_plan_dropped_with_kernel_choice(cuda):
 
 @pytest.mark.parametrize("case,expect", [("stencil27", "rows"), ("laplacian", "rows"), ("banded", "rows"),
                                          ("power_law", "segments"), ("long_rows", "split"),
-                                         ("empty_rows", "segments"), ("huge_row", "split")])
+                                         ("empty_rows", "segments"), ("huge_row", "split"),
+                                         ("scattered12", "gather"), ("scattered24", "segments")])
 def test_csr_kernel_choice(cuda, case, expect):
     A = mgb.matrix_from_host(_csr_case(case, np.float64), device="cuda")
-    want = {"rows": mgb.CSR_ROWS, "segments": mgb.CSR_SEGMENTS, "split": mgb.CSR_SPLIT}[expect]
+    want = {"rows": mgb.CSR_ROWS, "segments": mgb.CSR_SEGMENTS, "split": mgb.CSR_SPLIT,
+            "gather": mgb.CSR_ROWS_GATHER}[expect]
     assert A.kernel_variant() == want
 
 
