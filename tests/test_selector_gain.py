@@ -12,11 +12,14 @@ is the network trained on the training part.  Both were written by one run of
 On the held-out matrices the learned choice must stay within 10 % of the
 exhaustive best time on average (mean regret), capture at least 90 % of the
 exhaustive oracle's (log) speed-up over CSR only, and beat the rule-based
-selector whose thresholds are tuned on the same training matrices.  (The
-absolute speed-up over CSR only is bounded by the oracle's: with the
-adaptive-chunk CSR kernel the best format is 1.42x faster than CSR on this
-corpus in geometric mean.)  The CPU test runs the network through the FP64
-oracle; the GPU test through the library's forward kernel.
+selector whose thresholds are tuned on the same training matrices.  The
+absolute speed-up over CSR only is bounded by the oracle's, which shrinks as
+the CSR kernels get faster: with the chunk-planned lane-segment kernel and
+the reworked row-tile kernels the best format is 1.23x faster than CSR on
+this corpus in geometric mean (1.42x with the earlier CSR kernels, 1.64x
+before the adaptive chunk size), so the absolute bar is 1.15x.  The CPU test
+runs the network through the FP64 oracle; the GPU test through the
+library's forward kernel.
 """
 import os
 
@@ -49,7 +52,7 @@ def _check_gain(choice, c):
     assert learned["mean_regret"] <= 0.10, learned
     oracle = learned["oracle_geomean_speedup_vs_csr"]
     assert np.log(learned["geomean_speedup_vs_csr"]) >= 0.9 * np.log(oracle), learned
-    assert learned["geomean_speedup_vs_csr"] >= 1.3, learned
+    assert learned["geomean_speedup_vs_csr"] >= 1.15, learned
     assert learned["mean_regret"] < rule["mean_regret"], (learned, rule)
     assert learned["geomean_speedup_vs_csr"] > rule["geomean_speedup_vs_csr"], (learned, rule)
     return learned, rule
