@@ -43,9 +43,9 @@ namespace {
 
 constexpr int CSR_WARPS = 8;  // warps per CTA
 
-// DOT: also x[0..nrows) . y of the finished rows, one partial per warp in
-// partials[blockIdx.x * CSR_WARPS + warp] (the fused step of an iterative
-// solver; the matrix is square there).  With a chunk plan the warps read
+// DOT: also x[0..nrows) . y of the finished rows, one partial per CTA in
+// partials[blockIdx.x] (the fused step of an iterative solver; the matrix is
+// square there; the launcher caps the grid at the resident CTAs).  With a chunk plan the warps read
 // their rows from it instead of searching the row offsets.
 template <typename T, bool DOT>
 __global__ void __launch_bounds__(CSR_WARPS * 32, 3)
@@ -68,8 +68,16 @@ spmv_csr_segments(int64_t nrows, int64_t ncols, int64_t nnz, int64_t nchunks, in
     }
   }
   if (DOT) {
+    __shared__ T s_part[CSR_WARPS];
     part = warp_sum(part);
-    if (lane == 0) partials[(int64_t)blockIdx.x * CSR_WARPS + w] = part;
+    if (lane == 0) s_part[w] = part;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      T t = T(0);
+#pragma unroll
+      for (int i = 0; i < CSR_WARPS; i++) t += s_part[i];
+      partials[blockIdx.x] = t;
+    }
   }
 }
 
@@ -231,7 +239,11 @@ int launch_csr_dot(const mgb_csr* A, const T* x, T* y, int init, void* stream, i
   MGB_REQUIRE(plan == nullptr || plan_entries == nchunks + 1, MGB_ERR_BAD_ARGUMENT);
   int64_t blocks = (nchunks + CSR_WARPS - 1) / CSR_WARPS;
   if (blocks > 0x7fffffffLL) blocks = 0x7fffffffLL;
-  if (npartials) *npartials = blocks * CSR_WARPS;
+  if (npartials || partials) {  // the fused dot: one partial per CTA, grid capped at the resident CTAs
+    const int64_t resident = (int64_t)num_sms() * 3;
+    if (blocks > resident) blocks = resident;
+    if (npartials) *npartials = blocks;
+  }
   if (npartials && !partials) return MGB_SUCCESS;
   if (partials)
     spmv_csr_segments<T, true><<<(unsigned)blocks, CSR_WARPS * 32, 0, as_stream(stream)>>>(

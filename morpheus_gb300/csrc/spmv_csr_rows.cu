@@ -70,8 +70,9 @@ __device__ __forceinline__ void rows_step(int32_t j, int32_t lo, int32_t hi, int
     if (lo + j + q < hi) acc = fmadd(vv[q], xv[q], acc);
 }
 
-// DOT: also x[0..nrows) . y, one partial per warp in
-// partials[blockIdx.x * ROWS_WARPS + warp].
+// DOT: also x[0..nrows) . y, one partial per CTA in partials[blockIdx.x]
+// (the launcher then caps the grid at the resident CTAs, so a solver sums a
+// few thousand partials, not one per tile).
 template <typename T, bool DOT, int TILE, int MINB>
 __global__ void __launch_bounds__(ROWS_WARPS * 32, MINB)
 spmv_csr_rowtile(int64_t nrows, int64_t ncols, const int32_t* __restrict__ ro, const int32_t* __restrict__ ci,
@@ -124,8 +125,16 @@ spmv_csr_rowtile(int64_t nrows, int64_t ncols, const int32_t* __restrict__ ro, c
     }
   }
   if (DOT) {
+    __shared__ T s_part[ROWS_WARPS];
     part = warp_sum(part);
-    if (lane == 0) partials[(int64_t)blockIdx.x * ROWS_WARPS + w] = part;
+    if (lane == 0) s_part[w] = part;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      T t = T(0);
+#pragma unroll
+      for (int i = 0; i < ROWS_WARPS; i++) t += s_part[i];
+      partials[blockIdx.x] = t;
+    }
   }
 }
 
@@ -163,9 +172,6 @@ __global__ void row_shape_kernel(const int32_t* __restrict__ ro, const int32_t* 
   }
 }
 
-// staging size of MGB_CSR_ROWS: the smallest of 224 / 448 / 896 entries that
-// holds a tile of 32 rows of the mean length (tiles longer than TILE are
-// processed in pieces, so this is a performance choice only)
 template <typename T, bool DOT, int TILE, int MINB>
 void launch_rows_cfg(const mgb_csr* A, const T* x, T* y, int init, cudaStream_t s, T* partials, unsigned blocks) {
   spmv_csr_rowtile<T, DOT, TILE, MINB><<<blocks, ROWS_WARPS * 32, 0, s>>>(
@@ -173,15 +179,29 @@ void launch_rows_cfg(const mgb_csr* A, const T* x, T* y, int init, cudaStream_t 
       partials);
 }
 
+// staging size of MGB_CSR_ROWS: the smallest of 224 / 448 / 896 entries that
+// holds a tile of 32 rows of the mean length (tiles longer than TILE are
+// processed in pieces, so this is a performance choice only); returns the
+// CTAs per SM of the chosen configuration
+int rows_config(const mgb_csr* A, bool gather, int* tile) {
+  const int64_t tile_entries = 32 * (A->nnz / (A->nrows > 0 ? A->nrows : 1)) + 8;
+  if (gather) { *tile = 224; return 10; }
+  if (tile_entries <= 224) { *tile = 224; return 12; }
+  if (tile_entries <= 448) { *tile = 448; return 10; }
+  *tile = 896;
+  return 5;
+}
+
 template <typename T, bool DOT>
 void launch_rows_variant(const mgb_csr* A, const T* x, T* y, int init, cudaStream_t s, T* partials,
                          unsigned blocks, bool gather) {
-  const int64_t tile_entries = 32 * (A->nnz / (A->nrows > 0 ? A->nrows : 1)) + 8;
+  int tile = 0;
+  rows_config(A, gather, &tile);
   if (gather)
     launch_rows_cfg<T, DOT, 224, 10>(A, x, y, init, s, partials, blocks);
-  else if (tile_entries <= 224)
+  else if (tile == 224)
     launch_rows_cfg<T, DOT, 224, 12>(A, x, y, init, s, partials, blocks);
-  else if (tile_entries <= 448)
+  else if (tile == 448)
     launch_rows_cfg<T, DOT, 448, 10>(A, x, y, init, s, partials, blocks);
   else
     launch_rows_cfg<T, DOT, 896, 5>(A, x, y, init, s, partials, blocks);
@@ -193,7 +213,13 @@ int launch_rows(const mgb_csr* A, const T* x, T* y, int init, cudaStream_t s, T*
   const int64_t ntiles = (A->nrows + 31) / 32;
   int64_t blocks = (ntiles + ROWS_WARPS - 1) / ROWS_WARPS;
   if (blocks > 0x7fffffffLL) blocks = 0x7fffffffLL;
-  if (npartials) *npartials = blocks * ROWS_WARPS;
+  if (npartials || partials) {
+    // the fused dot: one partial per CTA, grid capped at the resident CTAs
+    int tile = 0;
+    const int64_t resident = (int64_t)num_sms() * rows_config(A, gather, &tile);
+    if (blocks > resident) blocks = resident;
+    if (npartials) *npartials = blocks;
+  }
   if (npartials && !partials) return MGB_SUCCESS;
   if (partials)
     launch_rows_variant<T, true>(A, x, y, init, s, partials, (unsigned)blocks, gather);
