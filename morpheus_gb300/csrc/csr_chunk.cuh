@@ -169,7 +169,7 @@ __device__ __forceinline__ RowRange csr_rows_x(RowRange rows, int64_t nrows, int
     for (int k = 0; k < SEG; k++) {
       const int64_t e = la + s + k;
       const bool valid = e >= e_lo && e < lb;
-      while (valid && e >= re) {
+      while (valid && e >= re && r + 1 < r_end) {  // (the bound only matters for invalid offsets)
         if (rs >= e_lo) { y[r] = acc; } else { hrow = r; hval = acc; }
         r++;
         rs = re;
@@ -353,7 +353,7 @@ __device__ __forceinline__ void csr_split_chunk(int64_t k, int64_t chunk, int64_
     for (int q = 0; q < SEG; q++) {
       const int64_t e = la + s + q;
       const bool valid = e >= e_lo && e < lb;
-      while (valid && e >= re) {
+      while (valid && e >= re && r + 1 < r_hi) {  // (the bound only matters for invalid offsets)
         if (rs >= e_lo) { put(r, acc); } else { hrow = r; hval = acc; }
         r++;
         rs = re;
