@@ -81,12 +81,10 @@ spmv_batched_csr(const mgb_csr_batch_item* __restrict__ items, int64_t nitems, i
     if (lane == 0) g = atomicAdd(ws, 1);
     g = __shfl_sync(0xffffffffu, g, 0);
     if (g >= total) break;
-    // matrix owning chunk g: last i with prefix[i] <= g
-    int64_t lo = 0, hi = nitems - 1;
-    while (lo < hi) {
-      const int64_t mid = (lo + hi + 1) >> 1;
-      if (__ldg(prefix + mid) <= g) lo = mid; else hi = mid - 1;
-    }
+    // matrix owning chunk g: last i with prefix[i] <= g (a 32-ary search:
+    // the first i with prefix[i] > g, minus one; prefix[nitems] = total > g)
+    int64_t lo = csr::warp_lower_bound(prefix, 0, nitems, (int64_t)g + 1, lane) - 1;
+    lo = lo < 0 ? 0 : lo;
     const mgb_csr_batch_item it = items[lo];
     csr::csr_chunk<T, CHUNK, SEG>(g - __ldg(prefix + lo), it.nrows, it.ncols, it.row_offsets, it.column_indices,
                                   static_cast<const T*>(it.values), static_cast<const T*>(it.x),
