@@ -7,8 +7,13 @@ y = A*x over the whole matrix.  The 0.4 GB working set is larger than L2, so no
 flush is needed between steps.
 
     python bench.py [--gpus N --steps K --warmup W] [--impl reference]
-                    [--workload power_law|stencil27|laplacian] [--format csr|coo|dia|ell|hyb|hdc]
-                    [--dtype f64|f32] [--suite]
+                    [--workload power_law|stencil27|laplacian|uniform|batched|cg]
+                    [--format csr|coo|dia|ell|hyb|hdc] [--dtype f64|f32] [--size S]
+                    [--csr-kernel auto|segments|rows|gather|split]
+
+`uniform` is N rows of 12 distinct uniform random columns each (short equal
+rows with scattered x reads); `--csr-kernel` forces one CSR kernel instead of
+the library's per-matrix choice, to compare kernels on one matrix.
 
 Under torchrun (N > 1) every rank runs an independent replica (rows of
 different matrices are independent objects; no collective on the data path),
@@ -50,7 +55,11 @@ def peaks():
 # workloads
 # --------------------------------------------------------------------------
 
-DEFAULT_SIZE = {"power_law": 2_000_000, "stencil27": 160, "laplacian": 256}
+DEFAULT_SIZE = {"power_law": 2_000_000, "stencil27": 160, "laplacian": 256, "uniform": 2_000_000}
+
+
+UNIFORM_ROW_LEN = 12
+CSR_KERNELS = {"auto": None, "segments": 1, "rows": 2, "split": 3, "gather": 4}
 
 
 def build_workload(name: str, fmt: str, dtype, seed: int, size: int | None = None):
@@ -67,6 +76,8 @@ def build_workload(name: str, fmt: str, dtype, seed: int, size: int | None = Non
             A = gen.add_offband(A, 0.01, seed=seed + 1)
     elif name == "laplacian":
         A = gen.laplacian_2d(n, dtype=dtype)
+    elif name == "uniform":  # n rows of ROW_LEN distinct uniform random columns (scattered x reads)
+        A = gen.random_lengths_csr(n, n, np.full(n, UNIFORM_ROW_LEN), seed=seed, dtype=dtype)
     else:
         raise SystemExit(f"unknown workload {name}")
     if fmt == "csr":
@@ -252,7 +263,10 @@ def config_dict(args, hm):
             "l2": "inputs larger than L2 (no flush needed)" if args.workload != "laplacian"
             else "L2 flushed between steps (256 MB scratch write)",
             "parallelism": f"replicas x{args.gpus}",
-            **({"size": args.size} if getattr(args, "size", None) else {})}
+            **({"size": args.size} if getattr(args, "size", None) else {}),
+            **({"row_len": UNIFORM_ROW_LEN} if args.workload == "uniform" else {}),
+            **({"csr_kernel": args.csr_kernel}
+               if args.format == "csr" and getattr(args, "csr_kernel", "auto") != "auto" else {})}
 
 
 # --------------------------------------------------------------------------
@@ -275,6 +289,8 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
     A, hm = build_workload(args.workload, args.format, dtype, seed=rank, size=args.size)
     nbytes = algorithmic_bytes(hm, vbytes)
     M = mgb.matrix_from_host(hm, device=dev)
+    if args.format == "csr" and CSR_KERNELS[args.csr_kernel] is not None:
+        M._variant = CSR_KERNELS[args.csr_kernel]  # a forced CSR kernel (profiling comparisons)
     x_np = np.random.default_rng(1 + rank).uniform(-1, 1, hm["ncols"]).astype(dtype)
     x = torch.from_numpy(x_np).to(dev)
     y = torch.zeros(hm["nrows"], dtype=tdtype, device=dev)
@@ -705,7 +721,10 @@ def main():
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="mgb", choices=["mgb", "reference"])
-    ap.add_argument("--workload", default="power_law", choices=["power_law", "stencil27", "laplacian", "batched", "cg"])
+    ap.add_argument("--workload", default="power_law",
+                    choices=["power_law", "stencil27", "laplacian", "uniform", "batched", "cg"])
+    ap.add_argument("--csr-kernel", default="auto", choices=sorted(CSR_KERNELS),
+                    help="force one CSR kernel instead of the per-matrix choice (profiling)")
     ap.add_argument("--batch", type=int, default=4096)
     ap.add_argument("--size", type=int, default=None,
                     help="power-law rows / stencil or Laplacian grid edge (default: the benchmark size)")
