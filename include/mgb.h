@@ -128,8 +128,8 @@ int mgb_spmv_csr_f32(const mgb_csr* A, const float* x, float* y, int init, void*
  * MGB_CSR_ROWS for short rows of nearly equal length whose neighbouring rows
  * read neighbouring columns (stencils, banded and mesh matrices: the row-tile
  * kernel, coalesced x reads), MGB_CSR_ROWS_GATHER for short rows of nearly
- * equal length (at most 20) with scattered columns (the row-tile kernel with
- * small staging, leaving L1 to the x reads), MGB_CSR_SPLIT when some row is
+ * equal length with scattered columns (the row-tile kernel with a smaller
+ * shared-memory carve-out, leaving L1 to the x reads), MGB_CSR_SPLIT when some row is
  * longer than 8192 entries or rows average >= 512 (a row is then spread over
  * several warps instead of one: the reference's vector kernel gives a whole
  * row to one vector, impl/Csr/Kernels/Morpheus_Multiply_Impl.hpp), or
@@ -139,7 +139,7 @@ int mgb_spmv_csr_f32(const mgb_csr* A, const float* x, float* y, int init, void*
 #define MGB_CSR_SEGMENTS 1
 #define MGB_CSR_ROWS 2
 #define MGB_CSR_SPLIT 3 /* fixed nonzero chunks + carries: very long rows */
-#define MGB_CSR_ROWS_GATHER 4 /* row tiles, small staging: short rows, scattered columns */
+#define MGB_CSR_ROWS_GATHER 4 /* row tiles, more L1: short rows, scattered columns */
 int mgb_csr_choose_kernel(const mgb_csr* A, int* variant, void* stream);
 int mgb_spmv_csr_variant_f64(const mgb_csr* A, const double* x, double* y, int init, int variant, void* stream);
 int mgb_spmv_csr_variant_f32(const mgb_csr* A, const float* x, float* y, int init, int variant, void* stream);

@@ -11,8 +11,7 @@
 //                       length (longest row <= 28 and <= 1.5 x mean + 2):
 //   MGB_CSR_ROWS        when neighbouring rows read neighbouring columns
 //                       (stencils, banded matrices, FEM meshes), or
-//   MGB_CSR_ROWS_GATHER when their columns are scattered and rows are at
-//                       most 20 long, else
+//   MGB_CSR_ROWS_GATHER when their columns are scattered, else
 //   MGB_CSR_SEGMENTS    the lane-segment kernel of spmv_csr.cu (any structure).
 //
 // Row-tile kernel: one warp owns 32 consecutive rows.  The tile's entries are
@@ -20,19 +19,15 @@
 // staged into shared memory with cp.async (all in flight at once), then every
 // lane walks its own row from shared memory in lockstep with the others
 // (equal lengths keep every FP64 FMA full-warp), issuing its x reads 8, 4,
-// 2, 1 at a time so that FMA slots match the row length exactly.  The staging
-// size is a trade measured on GB300:
-//   * MGB_CSR_ROWS sizes TILE to hold a whole tile (32 x mean row length):
-//     224 / 448 / 896 entries with 12 / 10 / 5 CTAs of 4 warps per SM.  With
-//     neighbouring rows reading neighbouring x entries, a warp's x reads
-//     touch few sectors and more resident warps win (5-point Laplacian
-//     125 -> 69 us, 13-point band 96 -> 78 us).
-//   * MGB_CSR_ROWS_GATHER stages 224 entries at a time with 10 CTAs per SM,
-//     leaving about 140 KB of the SM's 256 KB for L1: scattered x reads need
-//     L1 lines to be in flight, and with 215 KB of shared memory the same
-//     kernel ran 2x slower (12 random entries per row: 213 -> 109 us, the
-//     lane-segment kernel 146 us).
-#include "mgb_internal.cuh"
+// 2, 1 at a time so that FMA slots match the row length exactly.  TILE holds
+// a whole tile (224 / 448 / 896 entries for 32 rows of the mean length), and
+// the two variants differ in CTAs per SM, i.e. in the shared-memory carve-out
+// and the L1 left beside it: neighbouring columns touch few x sectors and
+// want resident warps (about 172 KB of shared memory), scattered columns
+// need L1 lines for their misses in flight (about 129 KB; with 233 KB the
+// same kernel ran at half speed).  The measurements are at rows_config.
+#include <atomic>
+
 #include "mgb_internal.cuh"
 
 namespace mgb {
@@ -40,7 +35,6 @@ namespace {
 
 constexpr int ROWS_WARPS = 4;
 constexpr int ROWS_TILE_MAX = 896;  // 32 rows x 28 entries: the longest rows a tile is chosen for
-constexpr int ROWS_GATHER_MAX = 20;  // longest scattered rows MGB_CSR_ROWS_GATHER is chosen for
 
 __device__ __forceinline__ unsigned rows_smem_u32(const void* p) {
   return (unsigned)__cvta_generic_to_shared(p);
@@ -172,39 +166,70 @@ __global__ void row_shape_kernel(const int32_t* __restrict__ ro, const int32_t* 
   }
 }
 
+// Launches one staging configuration.  The shared-memory carve-out is set
+// to what MINB CTAs need (once per device): the driver would otherwise take
+// the largest carve-out that the CTAs fit, and the L1 left beside it is what
+// the x reads' misses in flight live in (measured: 12 scattered entries per
+// row, 448-entry staging, 10 CTAs: 213 us with a 233 KB carve-out, 110 us at
+// 6 CTAs in 129 KB).
 template <typename T, bool DOT, int TILE, int MINB>
-void launch_rows_cfg(const mgb_csr* A, const T* x, T* y, int init, cudaStream_t s, T* partials, unsigned blocks) {
+int launch_rows_cfg(const mgb_csr* A, const T* x, T* y, int init, cudaStream_t s, T* partials, unsigned blocks) {
+  static std::atomic<bool> carve_set[64];
+  int dev = 0;
+  MGB_CUDA_CHECK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64 || !carve_set[dev].load(std::memory_order_acquire)) {
+    constexpr int per_cta = ROWS_WARPS * TILE * (int)(sizeof(T) + sizeof(int32_t)) + 1024;
+    constexpr int pct = (MINB * per_cta * 100 + 228 * 1024 - 1) / (228 * 1024);
+    MGB_CUDA_CHECK(cudaFuncSetAttribute(spmv_csr_rowtile<T, DOT, TILE, MINB>,
+                                        cudaFuncAttributePreferredSharedMemoryCarveout, pct > 100 ? 100 : pct));
+    if (dev >= 0 && dev < 64) carve_set[dev].store(true, std::memory_order_release);
+  }
   spmv_csr_rowtile<T, DOT, TILE, MINB><<<blocks, ROWS_WARPS * 32, 0, s>>>(
       A->nrows, A->ncols, A->row_offsets, A->column_indices, static_cast<const T*>(A->values), x, y, init,
       partials);
+  return MGB_SUCCESS;
 }
 
-// staging size of MGB_CSR_ROWS: the smallest of 224 / 448 / 896 entries that
-// holds a tile of 32 rows of the mean length (tiles longer than TILE are
-// processed in pieces, so this is a performance choice only); returns the
-// CTAs per SM of the chosen configuration
+// CTAs per SM of a staging configuration: as many as fit a shared-memory
+// budget (180 KB for neighbouring columns: resident warps for the
+// latency-bound tiles; 135 KB for scattered columns: L1 for the misses in
+// flight), at most 12.  Measured on GB300 (us per SpMV, FP64, TILE x CTAs):
+//   5-point Laplacian 2048^2:      224 x 12  69.6
+//   band of 13, N = 2M:            448 x 10  78.5   448 x 8  71.7
+//   27-point stencil 160^3:        896 x 5  342.8   896 x 4  319.7   896 x 3  388.7
+//   scattered, 12 per row, N = 2M: 448 x 10 213.4   224 x 10 108.6   448 x 6 109.7
+//   scattered, 20 per row:         896 x 5  263.3   224 x 10 160.2   896 x 3 147.5
+//   scattered, 27 per row, N = 1M: 896 x 5  237.4   896 x 3  133.1   (lane segments 162)
+template <typename T>
+constexpr int rows_ctas(int tile, bool gather) {
+  const int per_cta = ROWS_WARPS * tile * (int)(sizeof(T) + sizeof(int32_t)) + 1024;
+  const int n = (gather ? 135 * 1024 : 180 * 1024) / per_cta;
+  return n > 12 ? 12 : (n < 1 ? 1 : n);
+}
+
+// Staging size: the smallest of 224 / 448 / 896 entries that holds a tile of
+// 32 rows of the mean length (longer tiles are processed in pieces, so this
+// is a performance choice only).  Returns the CTAs per SM of the choice.
+template <typename T>
 int rows_config(const mgb_csr* A, bool gather, int* tile) {
   const int64_t tile_entries = 32 * (A->nnz / (A->nrows > 0 ? A->nrows : 1)) + 8;
-  if (gather) { *tile = 224; return 10; }
-  if (tile_entries <= 224) { *tile = 224; return 12; }
-  if (tile_entries <= 448) { *tile = 448; return 10; }
-  *tile = 896;
-  return 5;
+  *tile = tile_entries <= 224 ? 224 : (tile_entries <= 448 ? 448 : 896);
+  return rows_ctas<T>(*tile, gather);
 }
 
 template <typename T, bool DOT>
-void launch_rows_variant(const mgb_csr* A, const T* x, T* y, int init, cudaStream_t s, T* partials,
-                         unsigned blocks, bool gather) {
+int launch_rows_variant(const mgb_csr* A, const T* x, T* y, int init, cudaStream_t s, T* partials,
+                        unsigned blocks, bool gather) {
   int tile = 0;
-  rows_config(A, gather, &tile);
-  if (gather)
-    launch_rows_cfg<T, DOT, 224, 10>(A, x, y, init, s, partials, blocks);
-  else if (tile == 224)
-    launch_rows_cfg<T, DOT, 224, 12>(A, x, y, init, s, partials, blocks);
-  else if (tile == 448)
-    launch_rows_cfg<T, DOT, 448, 10>(A, x, y, init, s, partials, blocks);
-  else
-    launch_rows_cfg<T, DOT, 896, 5>(A, x, y, init, s, partials, blocks);
+  rows_config<T>(A, gather, &tile);
+  if (gather) {
+    if (tile == 224) return launch_rows_cfg<T, DOT, 224, rows_ctas<T>(224, true)>(A, x, y, init, s, partials, blocks);
+    if (tile == 448) return launch_rows_cfg<T, DOT, 448, rows_ctas<T>(448, true)>(A, x, y, init, s, partials, blocks);
+    return launch_rows_cfg<T, DOT, 896, rows_ctas<T>(896, true)>(A, x, y, init, s, partials, blocks);
+  }
+  if (tile == 224) return launch_rows_cfg<T, DOT, 224, rows_ctas<T>(224, false)>(A, x, y, init, s, partials, blocks);
+  if (tile == 448) return launch_rows_cfg<T, DOT, 448, rows_ctas<T>(448, false)>(A, x, y, init, s, partials, blocks);
+  return launch_rows_cfg<T, DOT, 896, rows_ctas<T>(896, false)>(A, x, y, init, s, partials, blocks);
 }
 
 template <typename T>
@@ -216,15 +241,14 @@ int launch_rows(const mgb_csr* A, const T* x, T* y, int init, cudaStream_t s, T*
   if (npartials || partials) {
     // the fused dot: one partial per CTA, grid capped at the resident CTAs
     int tile = 0;
-    const int64_t resident = (int64_t)num_sms() * rows_config(A, gather, &tile);
+    const int64_t resident = (int64_t)num_sms() * rows_config<T>(A, gather, &tile);
     if (blocks > resident) blocks = resident;
     if (npartials) *npartials = blocks;
   }
   if (npartials && !partials) return MGB_SUCCESS;
-  if (partials)
-    launch_rows_variant<T, true>(A, x, y, init, s, partials, (unsigned)blocks, gather);
-  else
-    launch_rows_variant<T, false>(A, x, y, init, s, nullptr, (unsigned)blocks, gather);
+  const int st = partials ? launch_rows_variant<T, true>(A, x, y, init, s, partials, (unsigned)blocks, gather)
+                         : launch_rows_variant<T, false>(A, x, y, init, s, nullptr, (unsigned)blocks, gather);
+  if (st != MGB_SUCCESS) return st;
   MGB_LAUNCH_CHECK();
   return MGB_SUCCESS;
 }
@@ -254,8 +278,7 @@ int choose(const mgb_csr* A, int* variant, cudaStream_t s) {
   const double mean = (double)A->nnz / (double)A->nrows;
   const bool neighbouring = shape[2] == 0 || 2 * shape[1] >= shape[2];
   if (32 * mx <= ROWS_TILE_MAX && mx <= 1.5 * mean + 2.0) {
-    if (neighbouring) *variant = MGB_CSR_ROWS;
-    else if (mx <= ROWS_GATHER_MAX) *variant = MGB_CSR_ROWS_GATHER;
+    *variant = neighbouring ? MGB_CSR_ROWS : MGB_CSR_ROWS_GATHER;
   }
   // rows longer than a few chunks: one warp per row would be the critical
   // path (measured: a 150,000-entry row 746 -> 56 us; rows of 1,000-6,000

@@ -295,7 +295,7 @@ def test_chunk_plan_dropped_with_kernel_choice(cuda):
 @pytest.mark.parametrize("case,expect", [("stencil27", "rows"), ("laplacian", "rows"), ("banded", "rows"),
                                          ("power_law", "segments"), ("long_rows", "split"),
                                          ("empty_rows", "segments"), ("huge_row", "split"),
-                                         ("scattered12", "gather"), ("scattered24", "segments")])
+                                         ("scattered12", "gather"), ("scattered24", "gather")])
 def test_csr_kernel_choice(cuda, case, expect):
     A = mgb.matrix_from_host(_csr_case(case, np.float64), device="cuda")
     want = {"rows": mgb.CSR_ROWS, "segments": mgb.CSR_SEGMENTS, "split": mgb.CSR_SPLIT,
