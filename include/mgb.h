@@ -381,7 +381,8 @@ int mgb_coo_is_sorted(const mgb_coo* A, int* sorted, void* stream);
 /* ---- CSR SpMV from host memory --------------------------------------------
  * y = A*x (init) or y += A*x where the descriptor's arrays, x and y are HOST
  * pointers (pinned memory for overlap): the matrix is copied in nblocks
- * nnz-balanced row blocks (nblocks <= 0: 2; at most 64) and
+ * nnz-balanced row blocks (at most 64; nblocks <= 0: three blocks of 47 / 47 /
+ * 6 % of the nonzeros, so that little work is left after the last copy) and
  * block b is multiplied while block b+1 is in flight, y coming back per block.
  * The host-space counterpart of the reference's Serial / OpenMP multiply on
  * host containers (impl/Csr/Serial/Morpheus_Multiply_Impl.hpp:38-58).

@@ -90,18 +90,22 @@ int spmv_csr_host(const mgb_csr* A, const T* xh, T* yh, int init, int variant, i
   MGB_REQUIRE(ro_h[0] == 0 && (int64_t)ro_h[N] == nnz, MGB_ERR_INVALID_INPUT);
   const int32_t* ci_h = A->column_indices;
   const T* va_h = static_cast<const T*>(A->values);
-  // Default 2 blocks: measured on GB300 with a 405 MB power-law matrix,
-  // 1 / 2 / 4 / 8 / 16 blocks take 2.20 / 2.17 / 2.18 / 2.26 / 2.33 ms -- the
-  // host link (about 200 GB/s for these copies) dominates, the kernel hides
-  // behind the second block's copy, and more, smaller copies cost more.
-  if (nblocks <= 0) nblocks = 2;
+  // Only the last block's kernel and y copy are not hidden behind the
+  // host link, so by default the matrix goes in three blocks of 47 / 47 / 6 %
+  // of the nonzeros.  Measured on GB300 with a 405 MB power-law matrix:
+  // 1 / 2 / 4 / 8 / 16 equal blocks take 2.20 / 2.17 / 2.18 / 2.26 / 2.33 ms
+  // (more, smaller copies cost more); the tapered split: see the design notes.
+  // An explicit nblocks gives equal blocks.
+  const bool tapered = nblocks <= 0;
+  if (tapered) nblocks = 3;
   if (nblocks > N) nblocks = N;
   MGB_REQUIRE(nblocks <= MAX_BLOCKS, MGB_ERR_BAD_ARGUMENT);
   // nnz-balanced row boundaries
   int64_t rb[MAX_BLOCKS + 1];
   rb[0] = 0;
   for (int64_t b = 1; b < nblocks; b++) {
-    int64_t r = host_lower_bound(ro_h, N, nnz * b / nblocks);
+    const int64_t target = (tapered && nblocks == 3) ? (b == 1 ? nnz * 47 / 100 : nnz * 94 / 100) : nnz * b / nblocks;
+    int64_t r = host_lower_bound(ro_h, N, target);
     rb[b] = r < rb[b - 1] ? rb[b - 1] : r;
   }
   rb[nblocks] = N;
