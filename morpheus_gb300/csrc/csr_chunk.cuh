@@ -35,12 +35,12 @@ __device__ __forceinline__ int64_t warp_lower_bound(const int32_t* __restrict__ 
   return lo + __popc(__ballot_sync(0xffffffffu, less));
 }
 
-// Shared-memory staging of one warp.
-template <typename T, int SEG>
+// Shared-memory staging of one warp (RO: row offsets staged per chunk).
+template <typename T, int SEG, int RO = CSR_RO_STAGE>
 struct WarpStage {
   T val[32 * (SEG + 1)];
   int32_t col[32 * (SEG + 1)];
-  int32_t ro[CSR_RO_STAGE];
+  int32_t ro[RO];
 };
 
 // Rows [begin, end) of one warp chunk.
@@ -93,69 +93,72 @@ __device__ __forceinline__ RowRange planned_rows(int64_t wc, int64_t nrows, cons
 // rows is touched); the batched chunk-queue kernel, whose speed drops 12 %
 // with the extra bound (measured), walks unbounded and relies on valid
 // offsets, as the reference's kernels do.
-template <typename T, int SEG, typename XL, bool BOUNDED = true>
+// IDX: the type of entry and row indices inside the routine (int32_t is
+// exact when nnz < 2^31 - 4096, as the launchers require, and nrows < 2^31 -
+// 32); RO: row offsets staged per chunk.
+template <typename T, int SEG, typename XL, bool BOUNDED = true, typename IDX = int64_t, int RO = CSR_RO_STAGE>
 __device__ __forceinline__ RowRange csr_rows_x(RowRange rows, int64_t nrows, int64_t ncols,
                                                const int32_t* __restrict__ ro, const int32_t* __restrict__ ci,
                                                const T* __restrict__ va, XL xl, T* __restrict__ y, int init,
-                                               WarpStage<T, SEG>& stg, int lane) {
+                                               WarpStage<T, SEG, RO>& stg, int lane) {
   constexpr int CSR_PAD = SEG + 1;
   T* sv = stg.val;
   int32_t* sc = stg.col;
   int32_t* sro = stg.ro;
-  const int64_t r_begin = rows.begin, r_end = rows.end;
+  const IDX r_begin = (IDX)rows.begin, r_end = (IDX)rows.end;
   if (r_begin >= r_end) return RowRange{r_begin, r_begin};
-  const int64_t nr = r_end - r_begin;
-  const bool staged = nr < CSR_RO_STAGE;  // offsets r_begin..r_end in smem
+  const IDX nr = r_end - r_begin;
+  const bool staged = nr < RO;  // offsets r_begin..r_end in smem
   __syncwarp();
   if (staged)
-    for (int64_t i = lane; i <= nr; i += 32) sro[i] = __ldg(ro + r_begin + i);
+    for (IDX i = lane; i <= nr; i += 32) sro[i] = __ldg(ro + r_begin + i);
   __syncwarp();
-  auto ro_at = [&](int64_t i) -> int64_t {
-    return staged ? (int64_t)sro[i - r_begin] : (int64_t)__ldg(ro + i);
+  auto ro_at = [&](IDX i) -> IDX {
+    return staged ? (IDX)sro[i - r_begin] : (IDX)__ldg(ro + i);
   };
-  const int64_t E0 = ro_at(r_begin), E1 = ro_at(r_end);
+  const IDX E0 = ro_at(r_begin), E1 = ro_at(r_end);
   if (E0 >= E1) {  // only empty rows
     if (init)
-      for (int64_t r = r_begin + lane; r < r_end; r += 32) y[r] = T(0);
+      for (IDX r = r_begin + lane; r < r_end; r += 32) y[r] = T(0);
     return RowRange{r_begin, r_end};
   }
-  const int64_t A0 = E0 & ~(int64_t)7;  // 32-byte aligned column segments
-  int64_t KW = (E1 - A0 + 31) / 32;
+  const IDX A0 = E0 & ~(IDX)7;  // 32-byte aligned column segments
+  IDX KW = (E1 - A0 + 31) / 32;
   KW = (KW + SEG - 1) / SEG * SEG;
-  const int64_t la = A0 + lane * KW;
-  const int64_t lb = min(la + KW, E1);
-  const int64_t e_lo = max(la, E0);
+  const IDX la = A0 + lane * KW;
+  const IDX lb = min(la + KW, E1);
+  const IDX e_lo = max(la, E0);
   const bool active = e_lo < lb;
 
   // lane's first row: lane 0 starts at r_begin (so leading empty rows are
   // flushed); others at the row containing e_lo (empty rows sitting at a
   // lane boundary are flushed by the previous lane's tail loop).
-  int64_t r = r_end;
+  IDX r = r_end;
   if (active) {
     if (lane == 0) {
       r = r_begin;
     } else {
-      int64_t lo = r_begin, hi = r_end;  // first i in [lo, hi] with ro[i] > e_lo
+      IDX lo = r_begin, hi = r_end;  // first i in [lo, hi] with ro[i] > e_lo
       while (lo < hi) {
-        const int64_t mid = (lo + hi) >> 1;
+        const IDX mid = (lo + hi) >> 1;
         if (ro_at(mid) <= e_lo) lo = mid + 1; else hi = mid;
       }
       r = lo - 1;
     }
   }
-  int64_t rs = active ? ro_at(r) : 0;
-  int64_t re = active ? ro_at(r + 1) : 0;
+  IDX rs = active ? ro_at(r) : 0;
+  IDX re = active ? ro_at(r + 1) : 0;
   T acc = (active && rs >= e_lo && !init) ? y[r] : T(0);
-  int64_t hrow = -1;
+  IDX hrow = -1;
   T hval = T(0);
 
-  for (int64_t s = 0; s < KW; s += SEG) {
+  for (IDX s = 0; s < KW; s += SEG) {
     __syncwarp();
 #pragma unroll
     for (int q = 0; q < SEG; q++) {
       const int f = q * 32 + lane;
       const int L = f / SEG, j = f % SEG;
-      const int64_t e = A0 + L * KW + s + j;
+      const IDX e = A0 + L * KW + s + j;
       const bool in = e >= E0 && e < E1;
       sv[L * CSR_PAD + j] = in ? ldg_stream(va + e) : T(0);
       sc[L * CSR_PAD + j] = in ? ldg_stream(ci + e) : 0;
@@ -164,7 +167,7 @@ __device__ __forceinline__ RowRange csr_rows_x(RowRange rows, int64_t nrows, int
     T v[SEG], xv[SEG];
 #pragma unroll
     for (int k = 0; k < SEG; k++) {
-      const int64_t e = la + s + k;
+      const IDX e = la + s + k;
       const bool valid = e >= e_lo && e < lb;
       const int32_t c = sc[lane * CSR_PAD + k];
       v[k] = valid ? sv[lane * CSR_PAD + k] : T(0);
@@ -172,7 +175,7 @@ __device__ __forceinline__ RowRange csr_rows_x(RowRange rows, int64_t nrows, int
     }
 #pragma unroll
     for (int k = 0; k < SEG; k++) {
-      const int64_t e = la + s + k;
+      const IDX e = la + s + k;
       const bool valid = e >= e_lo && e < lb;
       while (valid && e >= re && (!BOUNDED || r + 1 < r_end)) {
         if (rs >= e_lo) { y[r] = acc; } else { hrow = r; hval = acc; }
@@ -200,16 +203,16 @@ __device__ __forceinline__ RowRange csr_rows_x(RowRange rows, int64_t nrows, int
   // the next lane; a row starting exactly at lb belongs to the next lane)
   // and segmented scan
   const bool has_tail = active && r < r_end && rs < lb;
-  const int64_t key = has_tail ? r : -1 - (int64_t)lane;
+  const IDX key = has_tail ? r : -1 - (IDX)lane;
   T cv = has_tail ? acc : T(0);
 #pragma unroll
   for (int d = 1; d < 32; d <<= 1) {
     const T u = __shfl_up_sync(0xffffffffu, cv, d);
-    const int64_t k2 = __shfl_up_sync(0xffffffffu, key, d);
+    const IDX k2 = __shfl_up_sync(0xffffffffu, key, d);
     if (lane >= d && k2 == key) cv += u;
   }
   const T vprev = __shfl_up_sync(0xffffffffu, cv, 1);
-  const int64_t kprev = __shfl_up_sync(0xffffffffu, key, 1);
+  const IDX kprev = __shfl_up_sync(0xffffffffu, key, 1);
   if (hrow >= 0) y[hrow] = (lane > 0 && kprev == hrow) ? hval + vprev : hval;
   return RowRange{r_begin, r_end};
 }

@@ -35,6 +35,8 @@
 //    forwards the partials, and the lane where the row ends adds them: 6
 //    extra FP64 warp instructions per ~2048 nonzeros.
 // With init == 0 a row's accumulator starts from y[i] (a load, no extra add).
+#include <type_traits>
+
 #include "csr_chunk.cuh"
 #include "primitives.cuh"
 
@@ -46,22 +48,27 @@ constexpr int CSR_WARPS = 8;  // warps per CTA
 // DOT: also x[0..nrows) . y of the finished rows, one partial per CTA in
 // partials[blockIdx.x] (the fused step of an iterative solver; the matrix is
 // square there; the launcher caps the grid at the resident CTAs).  With a chunk plan the warps read
-// their rows from it instead of searching the row offsets.
-template <typename T, bool DOT>
-__global__ void __launch_bounds__(CSR_WARPS * 32, 3)
+// their rows from it instead of searching the row offsets.  SMALL: 32-bit
+// indices in the chunk routine, 256 staged row offsets and 4 CTAs per SM
+// (64 registers) -- measured on GB300 faster for FP32 (power-law 183 ->
+// 164 us) and slower for FP64 (195 -> 206 us), so FP32 only.
+template <typename T, bool DOT, bool SMALL = false>
+__global__ void __launch_bounds__(CSR_WARPS * 32, SMALL ? 4 : 3)
 spmv_csr_segments(int64_t nrows, int64_t ncols, int64_t nnz, int64_t nchunks, int64_t chunk,
                   const int32_t* __restrict__ ro, const int32_t* __restrict__ ci,
                   const T* __restrict__ va, const T* __restrict__ x,
                   T* __restrict__ y, int init, T* __restrict__ partials, const int32_t* __restrict__ plan) {
-  __shared__ csr::WarpStage<T, csr::CSR_SEG> stage[CSR_WARPS];
+  constexpr int RO = SMALL ? 256 : csr::CSR_RO_STAGE;
+  using IDX = typename std::conditional<SMALL, int32_t, int64_t>::type;
+  __shared__ csr::WarpStage<T, csr::CSR_SEG, RO> stage[CSR_WARPS];
   const int lane = threadIdx.x & 31;
   const int w = threadIdx.x >> 5;
   T part = T(0);
   for (int64_t wc = (int64_t)blockIdx.x * CSR_WARPS + w; wc < nchunks;
        wc += (int64_t)gridDim.x * CSR_WARPS) {
     const csr::RowRange rows = plan ? csr::planned_rows(wc, nrows, plan) : csr::chunk_rows(wc, chunk, nrows, ro, lane);
-    const csr::RowRange rr = csr::csr_rows_x<T, csr::CSR_SEG>(rows, nrows, ncols, ro, ci, va, csr::XGlobal<T>{x}, y,
-                                                                init, stage[w], lane);
+    const csr::RowRange rr = csr::csr_rows_x<T, csr::CSR_SEG, csr::XGlobal<T>, true, IDX>(
+        rows, nrows, ncols, ro, ci, va, csr::XGlobal<T>{x}, y, init, stage[w], lane);
     if (DOT) {
       __syncwarp();  // the chunk's y entries, written by any lane, are visible to the warp
       for (int64_t r = rr.begin + lane; r < rr.end; r += 32) part = fmadd(x[r], y[r], part);
@@ -239,20 +246,31 @@ int launch_csr_dot(const mgb_csr* A, const T* x, T* y, int init, void* stream, i
   MGB_REQUIRE(plan == nullptr || plan_entries == nchunks + 1, MGB_ERR_BAD_ARGUMENT);
   int64_t blocks = (nchunks + CSR_WARPS - 1) / CSR_WARPS;
   if (blocks > 0x7fffffffLL) blocks = 0x7fffffffLL;
+  const bool small = sizeof(T) == 4 && A->nrows < 0x7fffff00LL;
   if (npartials || partials) {  // the fused dot: one partial per CTA, grid capped at the resident CTAs
-    const int64_t resident = (int64_t)num_sms() * 3;
+    const int64_t resident = (int64_t)num_sms() * (small ? 4 : 3);
     if (blocks > resident) blocks = resident;
     if (npartials) *npartials = blocks;
   }
   if (npartials && !partials) return MGB_SUCCESS;
-  if (partials)
-    spmv_csr_segments<T, true><<<(unsigned)blocks, CSR_WARPS * 32, 0, as_stream(stream)>>>(
-        A->nrows, A->ncols, A->nnz, nchunks, chunk, A->row_offsets, A->column_indices,
-        static_cast<const T*>(A->values), x, y, init, partials, plan);
+  const T* va = static_cast<const T*>(A->values);
+  const cudaStream_t s = as_stream(stream);
+  if (small && partials)
+    spmv_csr_segments<T, true, true><<<(unsigned)blocks, CSR_WARPS * 32, 0, s>>>(
+        A->nrows, A->ncols, A->nnz, nchunks, chunk, A->row_offsets, A->column_indices, va, x, y, init, partials,
+        plan);
+  else if (small)
+    spmv_csr_segments<T, false, true><<<(unsigned)blocks, CSR_WARPS * 32, 0, s>>>(
+        A->nrows, A->ncols, A->nnz, nchunks, chunk, A->row_offsets, A->column_indices, va, x, y, init, nullptr,
+        plan);
+  else if (partials)
+    spmv_csr_segments<T, true><<<(unsigned)blocks, CSR_WARPS * 32, 0, s>>>(
+        A->nrows, A->ncols, A->nnz, nchunks, chunk, A->row_offsets, A->column_indices, va, x, y, init, partials,
+        plan);
   else
-    spmv_csr_segments<T, false><<<(unsigned)blocks, CSR_WARPS * 32, 0, as_stream(stream)>>>(
-        A->nrows, A->ncols, A->nnz, nchunks, chunk, A->row_offsets, A->column_indices,
-        static_cast<const T*>(A->values), x, y, init, nullptr, plan);
+    spmv_csr_segments<T, false><<<(unsigned)blocks, CSR_WARPS * 32, 0, s>>>(
+        A->nrows, A->ncols, A->nnz, nchunks, chunk, A->row_offsets, A->column_indices, va, x, y, init, nullptr,
+        plan);
   MGB_LAUNCH_CHECK();
   return MGB_SUCCESS;
 }
