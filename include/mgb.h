@@ -284,7 +284,9 @@ int mgb_mlp_adam_f32(float* params, const float* grads, float* m, float* v, int6
  * array and needs no host synchronisation -- then launch as often as needed.
  * A launch is a memset of the work counter plus one kernel, so it can be
  * captured in a CUDA graph.  A launch whose config differs from the planned
- * one does nothing and sets workspace word 3 to 1.  Items must not share y. */
+ * one does nothing and sets workspace word 3 to 1.  Items must not share y,
+ * and each item must have nnz < 2^31 - 4096 and nrows < 2^31 - 32 (an item
+ * beyond that is skipped by the chunk-queue configs, which set word 3 to 3). */
 typedef struct mgb_csr_batch_item {
   int64_t nrows, ncols, nnz;
   int32_t* row_offsets;

@@ -97,7 +97,8 @@ class CsrBatch:
                   self.config, C.c_void_p(self._ws.data_ptr()), 1 if init else 0, _stream_handle(stream))
 
     def planned_ok(self) -> bool:
-        """False if a launch found the workspace planned for another config."""
+        """False if a launch found the workspace planned for another config, or
+        skipped an item too large for 32-bit indices (nnz >= 2^31 - 4096)."""
         return int(self._ws[12:16].view(torch.int32).item()) == 0
 
     def capture_graph(self, init: bool = True) -> torch.cuda.CUDAGraph:

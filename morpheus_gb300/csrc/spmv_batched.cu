@@ -86,6 +86,10 @@ spmv_batched_csr(const mgb_csr_batch_item* __restrict__ items, int64_t nitems, i
     int64_t lo = csr::warp_lower_bound(prefix, 0, nitems, (int64_t)g + 1, lane) - 1;
     lo = lo < 0 ? 0 : lo;
     const mgb_csr_batch_item it = items[lo];
+    if (it.nnz >= ((int64_t)1 << 31) - 4096 || it.nrows >= ((int64_t)1 << 31) - 32) {  // beyond 32-bit indices
+      if (lane == 0) ws[3] = 3;
+      continue;
+    }
     csr::csr_chunk<T, CHUNK, SEG>(g - __ldg(prefix + lo), it.nrows, it.ncols, it.row_offsets, it.column_indices,
                                   static_cast<const T*>(it.values), static_cast<const T*>(it.x),
                                   static_cast<T*>(it.y), init, stage[w], lane);
