@@ -560,7 +560,11 @@ def run_gpu_batched(args, rank: int, world: int, local_rank: int):
     xs = [torch.from_numpy(v).to(dev) for v in xs_np]
     ys = [torch.zeros(m["nrows"], dtype=dmats[0].dtype, device=dev) for m in mats]
     b = batched.CsrBatch(dmats, xs, ys)
-    best, tune_ms = b.autotune(reps=3, use_cache=False)
+    if args.batched_config is None:
+        best, tune_ms = b.autotune(reps=3, use_cache=False)
+    else:  # a fixed configuration (profiling comparisons): no autotuning launches
+        best, tune_ms = args.batched_config, None
+        b.plan(best)
     check_err = None
     if rank == 0 and not args.skip_check:
         from oracle import oracle as O
@@ -642,8 +646,9 @@ def run_gpu_batched(args, rank: int, world: int, local_rank: int):
                    "nnz_total": int(sum(m["nnz"] for m in mats)),
                    "rows_total": int(sum(m["nrows"] for m in mats)),
                    "l2": "inputs larger than L2 (no flush needed)", "parallelism": f"replicas x{world}",
-                   "autotuned_config": best, "config_chunk_seg": batched.config_info(best),
-                   "autotune_ms_per_config": tune_ms},
+                   ("autotuned_config" if tune_ms is not None else "fixed_config"): best,
+                   "config_chunk_seg": batched.config_info(best),
+                   **({"autotune_ms_per_config": tune_ms} if tune_ms is not None else {})},
         "pct_hbm_peak": 100.0 * achieved / peak, "rel_err_vs_oracle": check_err,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": batched_traffic(args), "peak_source": peak_src,
@@ -726,6 +731,8 @@ def main():
     ap.add_argument("--csr-kernel", default="auto", choices=sorted(CSR_KERNELS),
                     help="force one CSR kernel instead of the per-matrix choice (profiling)")
     ap.add_argument("--batch", type=int, default=4096)
+    ap.add_argument("--batched-config", type=int, default=None,
+                    help="batched workload: use this configuration instead of autotuning (profiling)")
     ap.add_argument("--size", type=int, default=None,
                     help="power-law rows / stencil or Laplacian grid edge (default: the benchmark size)")
     ap.add_argument("--format", default="csr", choices=["csr", "coo", "dia", "ell", "hyb", "hdc"])
