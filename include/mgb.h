@@ -171,7 +171,7 @@ int mgb_spmv_coo_f32(const mgb_coo* A, const float* x, float* y, int init, void*
 
 /* Allocation-free variant of mgb_spmv_coo_f64; it has no counterpart in the
  * reference.  For callers that may not allocate device memory while they run
- * (code inside an allocation-free graph-capture region, hosts that reserve all
+ * (real-time loops that forbid allocation once running, hosts that reserve all
  * device memory up front, plugins whose host owns the allocator): the carry
  * buffer is a fixed 4 MiB file-scope device array instead of cudaMallocAsync,
  * and no allocating call is made.  Limits: A->nnz <= 357,892,096, otherwise

@@ -240,10 +240,10 @@ int mgb_spmv_coo_f32(const mgb_coo* A, const float* x, float* y, int init, void*
 // ---------------------------------------------------------------------------
 // Allocation-free COO SpMV.
 //
-// For callers that cannot allocate device memory while they run: code inside
-// a CUDA-graph-captured region of a host application that forbids
-// allocations, real-time or embedded hosts that reserve all memory up front,
-// and plugins whose host process owns the allocator.  mgb_spmv_coo_f64 takes
+// For callers that cannot allocate device memory while they run: real-time
+// loops of a host application that forbids allocation once it is running,
+// embedded hosts that reserve all device memory up front, and plugins whose
+// host process owns the allocator.  mgb_spmv_coo_f64 takes
 // its carry buffer from cudaMallocAsync; this variant takes it from a fixed
 // file-scope device array instead, so it never calls cudaMalloc, cudaFree or
 // any allocating routine.

@@ -1,8 +1,8 @@
 """GPU: the allocation-free COO SpMV entry point (mgb_spmv_coo_f64_noalloc).
 
-Some callers cannot allocate device memory while they run -- code inside a
-graph-capture region of a host that forbids allocation, hosts that reserve all
-device memory up front, plugins whose host process owns the allocator.  For
+Some callers cannot allocate device memory while they run -- real-time loops
+of a host that forbids allocation once running, hosts that reserve all device
+memory up front, plugins whose host process owns the allocator.  For
 them the library offers one COO SpMV whose carry buffer is a fixed 4 MiB
 device array compiled into the library instead of stream-ordered scratch.
 
