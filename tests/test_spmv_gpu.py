@@ -144,6 +144,36 @@ def test_reference_multiply_check(cuda, N, dtype):
             assert err <= tol, f"{name} init={init}: max |dy| {err:.3e}"
 
 
+@pytest.mark.parametrize("N", [10, 100, 1000])
+def test_reference_multiply_dynamic_check(cuda, N):
+    """The reference's dynamic multiply test (core/tests/Test_Multiply_Dynamic.hpp:
+    46-271): one DynamicMatrix switched in place to every format in turn
+    (Test_Multiply_Dynamic.hpp:157-169; here the switch runs on the GPU,
+    where the reference's CUDA convert throws), multiplied through the
+    variant dispatch, same fixture, expected y and absolute bound as
+    test_reference_multiply_check (FP64)."""
+    hm = gen.banded(N, seed=N)
+    x = np.random.default_rng(5374857).uniform(-1.0, 1.0, N)
+    ro, ci, va = hm["row_offsets"], hm["column_indices"], hm["values"]
+    want = np.zeros(N)
+    for r in range(N):
+        s = 0.0
+        for j in range(ro[r], ro[r + 1]):
+            s = s + float(va[j]) * float(x[ci[j]])
+        want[r] = s
+    dyn = mgb.DynamicMatrix(mgb.matrix_from_host(hm, device="cuda"))
+    xt = torch.from_numpy(x).cuda()
+    for f in range(len(FORMATS)):
+        st = mgb.convert(dyn, f)
+        if st != mgb.conversion_error_e.CONV_SUCCESS:
+            continue  # the fill rule refuses DIA / ELL for this matrix, as the reference's convert does
+        assert dyn.active_index() == f
+        y = torch.zeros(N, dtype=torch.float64, device="cuda")
+        mgb.multiply(dyn, xt, y)
+        err = float(np.max(np.abs(y.cpu().numpy() - want)))
+        assert err <= 1e-13, f"{FORMATS[f]}: max |dy| {err:.3e}"
+
+
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
 def test_power_law_small(cuda, dtype):
     A = gen.power_law(30000, seed=3, dtype=dtype)
