@@ -177,7 +177,9 @@ int mgb_spmv_coo_f32(const mgb_coo* A, const float* x, float* y, int init, void*
  * and no allocating call is made.  Limits: A->nnz <= 357,892,096, otherwise
  * MGB_ERR_INVALID_INPUT before any work is queued; every GPU that loads the
  * library holds the 4 MiB until exit; the first call on a device looks up the
- * array's address (make it before any stream capture); all calls share the
+ * array's address (make it before any stream capture), and so does the first
+ * call after the current CUDA context changed (cudaDeviceReset, or another
+ * context made current through the driver API); all calls share the
  * array, so calls overlapping on the GPU race -- serialise them.  Same result
  * as mgb_spmv_coo_f64. */
 int mgb_spmv_coo_f64_noalloc(const mgb_coo* A, const double* x, double* y, int init, void* stream);
@@ -282,11 +284,14 @@ int mgb_mlp_adam_f32(float* params, const float* grads, float* m, float* v, int6
  * counter.  Usage: allocate mgb_spmv_batched_csr_workspace_bytes() of device
  * memory, plan once per (batch, config) -- the plan reads the device item
  * array and needs no host synchronisation -- then launch as often as needed.
- * A launch is a memset of the work counter plus one kernel, so it can be
- * captured in a CUDA graph.  A launch whose config differs from the planned
- * one does nothing and sets workspace word 3 to 1.  Items must not share y,
- * and each item must have nnz < 2^31 - 4096 and nrows < 2^31 - 32 (an item
- * beyond that is skipped by the chunk-queue configs, which set word 3 to 3). */
+ * A launch is two memsets (work counter, error flag) plus one kernel, so it
+ * can be captured in a CUDA graph.  Workspace word 3 reports the last launch:
+ * 0 when it ran, 1 when its config differs from the planned one (it did
+ * nothing).  Items must not share y, and each item must have nnz < 2^31 - 4096
+ * and nrows < 2^31 - 32 (an item beyond that is skipped by the chunk-queue
+ * configs, which set word 3 to 3).  A chunk-queue plan whose chunk total
+ * exceeds 2^31 - 1 is recorded for no config (word 3 = 4 after the plan),
+ * so every later launch does nothing and sets word 3 to 1. */
 typedef struct mgb_csr_batch_item {
   int64_t nrows, ncols, nnz;
   int32_t* row_offsets;

@@ -97,12 +97,13 @@ class CsrBatch:
                   self.config, C.c_void_p(self._ws.data_ptr()), 1 if init else 0, _stream_handle(stream))
 
     def planned_ok(self) -> bool:
-        """False if a launch found the workspace planned for another config, or
-        skipped an item too large for 32-bit indices (nnz >= 2^31 - 4096)."""
+        """False if the last launch found the workspace planned for another
+        config (or for none: a chunk total beyond 2^31 - 1), or skipped an
+        item too large for 32-bit indices (nnz >= 2^31 - 4096)."""
         return int(self._ws[12:16].view(torch.int32).item()) == 0
 
     def capture_graph(self, init: bool = True) -> torch.cuda.CUDAGraph:
-        """The batched launch (counter memset + kernel) captured as a CUDA graph."""
+        """The batched launch (two memsets + kernel) captured as a CUDA graph."""
         if self.config is None:
             self.plan(2)
         s = torch.cuda.Stream(device=self.device)

@@ -9,6 +9,7 @@
 namespace mgb {
 
 static thread_local char g_last_cuda_error[256] = "no error";
+static thread_local bool g_device_query_failed = false;
 
 int record_cuda_error(cudaError_t e) {
   std::snprintf(g_last_cuda_error, sizeof(g_last_cuda_error), "%s: %s",
@@ -20,16 +21,37 @@ int num_sms() {
   // per-device cache; atomics because several host threads may call at once
   static std::atomic<int> cache[64];
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return 152;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) {
+    record_cuda_error(e);
+    g_device_query_failed = true;
+    return 1;
+  }
   const bool cacheable = dev >= 0 && dev < 64;
   if (cacheable) {
     const int c = cache[dev].load(std::memory_order_relaxed);
-    if (c > 0) return c;
+    if (c > 0) {
+      g_device_query_failed = false;
+      return c;
+    }
   }
   int n = 0;
-  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 152;
+  e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess || n <= 0) {
+    if (e != cudaSuccess) record_cuda_error(e);
+    else std::snprintf(g_last_cuda_error, sizeof(g_last_cuda_error), "device %d reports %d SMs", dev, n);
+    g_device_query_failed = true;
+    return 1;
+  }
   if (cacheable) cache[dev].store(n, std::memory_order_relaxed);
+  g_device_query_failed = false;
   return n;
+}
+
+int take_device_query_error() {
+  if (!g_device_query_failed) return MGB_SUCCESS;
+  g_device_query_failed = false;
+  return MGB_ERR_CUDA;
 }
 
 }  // namespace mgb

@@ -14,8 +14,13 @@ int record_cuda_error(cudaError_t e);
 
 // Number of SMs of the current device (queried once per device and cached,
 // unlike the reference which queries device properties on every launch,
-// impl/Morpheus_CudaUtils.hpp:77-90).
+// impl/Morpheus_CudaUtils.hpp:77-90).  If the query fails it records the CUDA
+// error, returns 1 (a grid that is still valid) and flags the failure for
+// take_device_query_error(), which MGB_LAUNCH_CHECK consults: the entry point
+// then returns MGB_ERR_CUDA instead of running on a guessed SM count.
 int num_sms();
+// MGB_ERR_CUDA once after a failed num_sms() query on this thread, else MGB_SUCCESS.
+int take_device_query_error();
 
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
@@ -27,7 +32,12 @@ inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s
     if (mgb_e_ != cudaSuccess) return ::mgb::record_cuda_error(mgb_e_); \
   } while (0)
 
-#define MGB_LAUNCH_CHECK() MGB_CUDA_CHECK(cudaGetLastError())
+#define MGB_LAUNCH_CHECK()                                          \
+  do {                                                              \
+    MGB_CUDA_CHECK(cudaGetLastError());                             \
+    const int mgb_q_ = ::mgb::take_device_query_error();            \
+    if (mgb_q_ != MGB_SUCCESS) return mgb_q_;                       \
+  } while (0)
 
 #define MGB_REQUIRE(cond, status) \
   do {                            \

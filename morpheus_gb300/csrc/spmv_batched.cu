@@ -55,11 +55,15 @@ __global__ void batch_chunk_counts(const mgb_csr_batch_item* __restrict__ items,
     counts[i] = (int32_t)(items[i].nnz / chunk + 1);
 }
 
+// A chunk total beyond int32 cannot be indexed by the chunk queue: the plan
+// is then recorded for no configuration (-1), so every launch sets the error
+// flag and does nothing.
 __global__ void batch_finish_plan(int32_t* ws, const int64_t* total, int config) {
+  const bool fits = *total <= (int64_t)0x7fffffff;
   ws[0] = 0;
-  ws[1] = (int32_t)*total;
-  ws[2] = config;
-  ws[3] = 0;
+  ws[1] = fits ? (int32_t)*total : 0;
+  ws[2] = fits ? config : -1;
+  ws[3] = fits ? 0 : 4;
 }
 
 template <typename T, int CFG>
@@ -326,7 +330,8 @@ int launch(const mgb_csr_batch_item* items, int64_t nitems, int config, void* wo
   MGB_REQUIRE(items != nullptr && workspace != nullptr && nitems > 0, MGB_ERR_BAD_ARGUMENT);
   MGB_REQUIRE(config >= 0 && config < BAT_NCONFIGS, MGB_ERR_BAD_ARGUMENT);
   int32_t* ws = static_cast<int32_t*>(workspace);
-  MGB_CUDA_CHECK(cudaMemsetAsync(ws, 0, sizeof(int32_t), s));  // work counter
+  MGB_CUDA_CHECK(cudaMemsetAsync(ws, 0, sizeof(int32_t), s));      // work counter
+  MGB_CUDA_CHECK(cudaMemsetAsync(ws + 3, 0, sizeof(int32_t), s));  // error flag: reports this launch only
   switch (config) {
     case 0: return launch_cfg<T, 0>(items, nitems, ws, init, s);
     case 1: return launch_cfg<T, 1>(items, nitems, ws, init, s);

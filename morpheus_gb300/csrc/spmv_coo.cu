@@ -256,12 +256,19 @@ int mgb_spmv_coo_f32(const mgb_coo* A, const float* x, float* y, int init, void*
 //    work is queued.
 //  * The first call on a device looks up the array's device address with
 //    cudaGetSymbolAddress (once per device, with that device current) and
-//    caches it; make that first call before any stream capture.
+//    caches it with the unique ID of the current CUDA context; make that
+//    first call before any stream capture.  A later call that finds another
+//    context current (after cudaDeviceReset, or a context the caller made
+//    current through the driver API) looks the address up again, so the
+//    first call in each new context is a set-up call too.  Where the driver
+//    gives no context ID, every call looks the address up.
 //  * Every call uses the same array and leaves the previous call's carries
 //    in it.  Nothing in it needs to start at zero: each call writes every
 //    carry slot it reads.  Calls that overlap on the GPU (other streams, other
 //    host threads) race on the array; serialise them.
 // ---------------------------------------------------------------------------
+#include <cuda.h>  // CUcontext / CUresult types only: the driver calls are resolved at run time
+
 #include <mutex>
 
 namespace mgb {
@@ -275,23 +282,59 @@ static __device__ __align__(256) unsigned char g_coo_noalloc_scratch[mgb::COO_NO
 namespace mgb {
 namespace {
 
+struct NoallocSlot {
+  unsigned long long ctx_id;  // unique ID of the context the address belongs to (0: none)
+  void* ptr;
+};
 std::mutex g_noalloc_mutex;
-void* g_noalloc_ptr[128] = {};
+NoallocSlot g_noalloc[128] = {};
 
-// Device address of the scratch array for the current device (set-up on the
-// first call per device).
+// cuCtxGetCurrent / cuCtxGetId through the runtime's driver entry points (no
+// link against the driver library).  Context IDs are unique for the life of
+// the process, unlike context handles, which a new context may reuse.
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+unsigned long long current_ctx_id() {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<CtxGetIdFn>(f);
+  });
+  CUcontext c = nullptr;
+  unsigned long long id = 0;
+  if (get_current == nullptr || get_id == nullptr || get_current(&c) != CUDA_SUCCESS || c == nullptr ||
+      get_id(c, &id) != CUDA_SUCCESS)
+    return 0;
+  return id;
+}
+
+// Device address of the scratch array in the current context: looked up on
+// the first call per device and again whenever the current context changed.
 int noalloc_scratch(void** out) {
   int dev = 0;
   MGB_CUDA_CHECK(cudaGetDevice(&dev));
   MGB_REQUIRE(dev >= 0 && dev < 128, MGB_ERR_RUNTIME);
   std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (g_noalloc_ptr[dev] == nullptr) {
+  NoallocSlot& slot = g_noalloc[dev];
+  const unsigned long long id = current_ctx_id();
+  if (slot.ptr == nullptr || id == 0 || slot.ctx_id != id) {
     void* p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_coo_noalloc_scratch);
     if (e != cudaSuccess) return record_cuda_error(e);
-    g_noalloc_ptr[dev] = p;
+    slot.ptr = p;
+    slot.ctx_id = id != 0 ? id : current_ctx_id();  // the look-up may have created the context
   }
-  *out = g_noalloc_ptr[dev];
+  *out = slot.ptr;
   return MGB_SUCCESS;
 }
 

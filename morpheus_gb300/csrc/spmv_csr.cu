@@ -156,7 +156,7 @@ template <typename T>
 int launch_split(const mgb_csr* A, const T* x, T* y, int init, cudaStream_t s, T* partials, int64_t* npartials) {
   const int64_t dot_blocks = (int64_t)num_sms() * 4;
   if (npartials) *npartials = dot_blocks;
-  if (npartials && !partials) return MGB_SUCCESS;
+  if (npartials && !partials) return take_device_query_error();
   if (A->nnz == 0) {
     if (init) MGB_CUDA_CHECK(cudaMemsetAsync(y, 0, sizeof(T) * A->nrows, s));
   } else {
@@ -252,7 +252,7 @@ int launch_csr_dot(const mgb_csr* A, const T* x, T* y, int init, void* stream, i
     if (blocks > resident) blocks = resident;
     if (npartials) *npartials = blocks;
   }
-  if (npartials && !partials) return MGB_SUCCESS;
+  if (npartials && !partials) return take_device_query_error();
   const T* va = static_cast<const T*>(A->values);
   const cudaStream_t s = as_stream(stream);
   if (small && partials)
@@ -302,7 +302,7 @@ int mgb_spmv_csr_variant_f32(const mgb_csr* A, const float* x, float* y, int ini
 int mgb_csr_plan_entries(const mgb_csr* A, int64_t* entries) {
   if (A == nullptr || entries == nullptr || mgb::bad_sizes(A->nrows, A->ncols, A->nnz)) return MGB_ERR_BAD_ARGUMENT;
   *entries = A->nnz / mgb::segments_chunk(A) + 2;
-  return MGB_SUCCESS;
+  return mgb::take_device_query_error();
 }
 
 int mgb_csr_plan(const mgb_csr* A, int32_t* plan, int64_t entries, void* stream) {

@@ -245,7 +245,7 @@ int launch_rows(const mgb_csr* A, const T* x, T* y, int init, cudaStream_t s, T*
     if (blocks > resident) blocks = resident;
     if (npartials) *npartials = blocks;
   }
-  if (npartials && !partials) return MGB_SUCCESS;
+  if (npartials && !partials) return take_device_query_error();
   const int st = partials ? launch_rows_variant<T, true>(A, x, y, init, s, partials, (unsigned)blocks, gather)
                          : launch_rows_variant<T, false>(A, x, y, init, s, nullptr, (unsigned)blocks, gather);
   if (st != MGB_SUCCESS) return st;

@@ -163,12 +163,15 @@ int spmv_csr_host(const mgb_csr* A, const T* xh, T* yh, int init, int variant, i
   if (ce == cudaSuccess && status == MGB_SUCCESS) ce = cudaEventRecord(ev[nblocks + 1], k);
   if (ce == cudaSuccess && status == MGB_SUCCESS) ce = cudaStreamWaitEvent(s, ev[nblocks + 1], 0);
   // the caller's stream now orders after every copy and kernel; wait for
-  // the host-visible y (and for k, so scratch is released in stream order)
+  // the host-visible y (and for k, so scratch is released in stream order).
+  // Both streams are drained on every path, errors included: copies queued
+  // on s read the caller's host buffers, which it may reuse once we return.
   const cudaError_t ce_sync = k ? cudaStreamSynchronize(k) : cudaSuccess;
+  const cudaError_t ce_sync_s = cudaStreamSynchronize(s);
   if (status != MGB_SUCCESS) return status;
   if (ce != cudaSuccess) return record_cuda_error(ce);
   if (ce_sync != cudaSuccess) return record_cuda_error(ce_sync);
-  MGB_CUDA_CHECK(cudaStreamSynchronize(s));
+  if (ce_sync_s != cudaSuccess) return record_cuda_error(ce_sync_s);
   return MGB_SUCCESS;
 }
 

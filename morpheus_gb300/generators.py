@@ -126,17 +126,34 @@ def add_offband(A: dict, frac: float = 0.01, seed: int = 1) -> dict:
     rng = _rng(seed)
     N, M = A["nrows"], A["ncols"]
     ro = A["row_offsets"].astype(np.int64)
-    rows0 = np.repeat(np.arange(N, dtype=np.int64), np.diff(ro))
-    keys0 = rows0 * M + A["column_indices"].astype(np.int64)
+    cols0 = A["column_indices"]
     extra = int(round(frac * A["nnz"]))
     new = np.unique(rng.integers(0, N, extra, dtype=np.int64) * M + rng.integers(0, M, extra, dtype=np.int64))
-    new = new[~np.isin(new, keys0, assume_unique=False)]
-    keys = np.concatenate([keys0, new])
-    vals = np.concatenate([A["values"], _nonzero_normal(rng, new.size, A["values"].dtype)])
-    order = np.argsort(keys, kind="stable")
-    keys, vals = keys[order], vals[order]
-    rows = keys // M
-    return csr_from_sorted_keys(N, M, rows, keys - rows * M, vals)
+    nr = new // M
+    nc = new - nr * M
+    # rows are sorted by column: a vectorised binary search in each new
+    # entry's row gives its merge position and whether (r, c) is occupied
+    lo, hi = ro[nr], ro[nr + 1]
+    while True:
+        act = lo < hi
+        if not act.any():
+            break
+        mid = (lo + hi) // 2
+        go_right = act & (cols0[np.minimum(mid, max(A["nnz"] - 1, 0))] < nc)
+        lo = np.where(go_right, mid + 1, lo)
+        hi = np.where(act & ~go_right, mid, hi)
+    hit = lo < ro[nr + 1]
+    hit[hit] = cols0[lo[hit]] == nc[hit]
+    keep = ~hit
+    nr, nc, at = nr[keep], nc[keep], lo[keep]
+    new_vals = _nonzero_normal(rng, nr.size, A["values"].dtype)
+    ro_new = ro.copy()
+    ro_new[1:] += np.cumsum(np.bincount(nr, minlength=N))
+    # at is non-decreasing and np.insert keeps equal positions in the given order
+    cols = np.insert(cols0, at, nc.astype(np.int32))
+    vals = np.insert(A["values"], at, new_vals)
+    return {"format": CSR, "nrows": int(N), "ncols": int(M), "nnz": int(cols.size),
+            "row_offsets": ro_new.astype(np.int32), "column_indices": cols, "values": vals}
 
 
 def banded(N: int, diag_freq: int = 5, seed: int = 0, dtype=np.float64) -> dict:
