@@ -792,9 +792,31 @@ bool is_sorted(const CooMatrix<ValueType>& A) {
 }
 
 // ------------------------------------------------------------ analytics ---
-// core/src/Morpheus_MatrixAnalytics.hpp:49-261 on the device.  CSR and COO
-// are counted directly; other formats go through COO first.
+// core/src/Morpheus_MatrixAnalytics.hpp:49-261 on the device, every format
+// read in place with the reference's per-format counting rules (mgb.h).
 namespace Impl {
+// typed entry points (DIA / ELL / HYB / HDC per-diagonal counts read values;
+// DIA / HDC features too)
+template <class T> struct CountAbi;
+#define MGB_COUNT_ENTRIES(sfx)                                                                                 \
+  static int diag(const mgb_dia* a, int32_t* o, int i) { return mgb_count_nnz_per_diagonal_dia_##sfx(a, o, i, nullptr); } \
+  static int diag(const mgb_ell* a, int32_t* o, int i) { return mgb_count_nnz_per_diagonal_ell_##sfx(a, o, i, nullptr); } \
+  static int diag(const mgb_hyb* a, int32_t* o, int i) { return mgb_count_nnz_per_diagonal_hyb_##sfx(a, o, i, nullptr); } \
+  static int diag(const mgb_hdc* a, int32_t* o, int i) { return mgb_count_nnz_per_diagonal_hdc_##sfx(a, o, i, nullptr); } \
+  static int features(const mgb_dia* a, float* f, uint8_t* m) { return mgb_features_dia_##sfx(a, f, m, nullptr); }       \
+  static int features(const mgb_hdc* a, float* f, uint8_t* m) { return mgb_features_hdc_##sfx(a, f, m, nullptr); }
+template <> struct CountAbi<double> { MGB_COUNT_ENTRIES(f64) };
+template <> struct CountAbi<float> { MGB_COUNT_ENTRIES(f32) };
+#undef MGB_COUNT_ENTRIES
+inline int features_of(const mgb_csr* a, float* f, uint8_t* m) { return mgb_features_csr(a, f, m, nullptr); }
+inline int features_of(const mgb_coo* a, float* f, uint8_t* m) { return mgb_features_coo(a, f, m, nullptr); }
+inline int features_of(const mgb_ell* a, float* f, uint8_t* m) { return mgb_features_ell(a, f, m, nullptr); }
+inline int features_of(const mgb_hyb* a, float* f, uint8_t* m) { return mgb_features_hyb(a, f, m, nullptr); }
+template <class T>
+int features_of_typed(const mgb_dia* a, float* f, uint8_t* m) { return CountAbi<T>::features(a, f, m); }
+template <class T>
+int features_of_typed(const mgb_hdc* a, float* f, uint8_t* m) { return CountAbi<T>::features(a, f, m); }
+
 template <class T>
 void count_rows(const CsrMatrix<T>& A, int32_t* out, bool init) {
   mgb_csr d = A.desc();
@@ -805,8 +827,26 @@ void count_rows(const CooMatrix<T>& A, int32_t* out, bool init) {
   mgb_coo d = A.desc();
   check(mgb_count_nnz_per_row_coo(&d, out, init, nullptr), "count_nnz_per_row<GB300>");
 }
-template <class M>
-void count_rows(const M& A, int32_t* out, bool init) { count_rows(to_coo(A), out, init); }
+template <class T>
+void count_rows(const DiaMatrix<T>& A, int32_t* out, bool init) {
+  mgb_dia d = A.desc();
+  check(mgb_count_nnz_per_row_dia(&d, out, init, nullptr), "count_nnz_per_row<GB300>");
+}
+template <class T>
+void count_rows(const EllMatrix<T>& A, int32_t* out, bool init) {
+  mgb_ell d = A.desc();
+  check(mgb_count_nnz_per_row_ell(&d, out, init, nullptr), "count_nnz_per_row<GB300>");
+}
+template <class T>
+void count_rows(const HybMatrix<T>& A, int32_t* out, bool init) {
+  mgb_hyb d = A.desc();
+  check(mgb_count_nnz_per_row_hyb(&d, out, init, nullptr), "count_nnz_per_row<GB300>");
+}
+template <class T>
+void count_rows(const HdcMatrix<T>& A, int32_t* out, bool init) {
+  mgb_hdc d = A.desc();
+  check(mgb_count_nnz_per_row_hdc(&d, out, init, nullptr), "count_nnz_per_row<GB300>");
+}
 template <class T>
 void count_rows(const DynamicMatrix<T>& A, int32_t* out, bool init) {
   std::visit([&](const auto& m) { count_rows(m, out, init); }, A.const_formats());
@@ -822,7 +862,10 @@ void count_diags(const CooMatrix<T>& A, int32_t* out, bool init) {
   check(mgb_count_nnz_per_diagonal_coo(&d, out, init, nullptr), "count_nnz_per_diagonal<GB300>");
 }
 template <class M>
-void count_diags(const M& A, int32_t* out, bool init) { count_diags(to_coo(A), out, init); }
+void count_diags(const M& A, int32_t* out, bool init) {  // DIA, ELL, HYB, HDC
+  const auto d = A.desc();
+  check(CountAbi<typename M::value_type>::diag(&d, out, init), "count_nnz_per_diagonal<GB300>");
+}
 template <class T>
 void count_diags(const DynamicMatrix<T>& A, int32_t* out, bool init) {
   std::visit([&](const auto& m) { count_diags(m, out, init); }, A.const_formats());
@@ -1006,25 +1049,35 @@ class FormatSelector {
     sigma_.assign(sigma);
   }
 
-  // The format the network picks for A (any container; non-CSR containers
-  // are converted to CSR on the device for the features).
-  template <class Matrix>
-  formats_e select(const Matrix& A) const {
-    using T = typename Matrix::value_type;
-    CsrMatrix<T> csr;
-    Impl::from_coo(Impl::to_coo(A), csr);
-    return select_csr(csr);
-  }
+  // The format the network picks for A (any container; its features are
+  // computed in place, the same in every format).
   template <class T>
-  formats_e select(const CsrMatrix<T>& A) const { return select_csr(A); }
-
- private:
-  template <class T>
-  formats_e select_csr(const CsrMatrix<T>& A) const {
+  formats_e select(const DiaMatrix<T>& A) const {
     std::vector<float> feat(12);
     std::vector<uint8_t> feas(6);
-    mgb_csr d = A.desc();
-    Impl::check(mgb_features_csr(&d, feat.data(), feas.data(), nullptr), "FormatSelector::select");
+    const mgb_dia d = A.desc();
+    Impl::check(Impl::features_of_typed<T>(&d, feat.data(), feas.data()), "FormatSelector::select");
+    return pick(feat, feas);
+  }
+  template <class T>
+  formats_e select(const HdcMatrix<T>& A) const {
+    std::vector<float> feat(12);
+    std::vector<uint8_t> feas(6);
+    const mgb_hdc d = A.desc();
+    Impl::check(Impl::features_of_typed<T>(&d, feat.data(), feas.data()), "FormatSelector::select");
+    return pick(feat, feas);
+  }
+  template <class Matrix>
+  formats_e select(const Matrix& A) const {  // CSR, COO, ELL, HYB
+    std::vector<float> feat(12);
+    std::vector<uint8_t> feas(6);
+    const auto d = A.desc();
+    Impl::check(Impl::features_of(&d, feat.data(), feas.data()), "FormatSelector::select");
+    return pick(feat, feas);
+  }
+
+ private:
+  formats_e pick(const std::vector<float>& feat, const std::vector<uint8_t>& feas) const {
     DeviceArray<float> X(feat), logp(6);
     DeviceArray<uint8_t> F(feas);
     Impl::check(mgb_mlp_forward_f32(params_.data(), mu_.data(), sigma_.data(), X.data(), F.data(), 1, logp.data(),

@@ -238,6 +238,20 @@ int mgb_waxpby_f32(int64_t n, float alpha, const float* x, float beta, const flo
  *   [10..13] 1 if DIA / ELL / HYB / HDC pass the reference fill-tolerance test
  * Synchronises the stream. */
 int mgb_analytics_csr(const mgb_csr* A, double* out14, void* stream);
+/* The same statistics for the other formats, read in place (no conversion):
+ * they describe the entries the matrix's COO form would hold -- every COO
+ * entry, DIA slots inside the matrix holding a nonzero value, ELL slots with
+ * a valid column -- so a matrix gives the same values whichever format is
+ * active.  The reference computes its analytics through count_nnz_per_row /
+ * count_nnz_per_diagonal of each format (core/src/Morpheus_MatrixAnalytics.hpp:85-261).
+ * DIA and HDC read values and come in both value types. */
+int mgb_analytics_coo(const mgb_coo* A, double* out14, void* stream);
+int mgb_analytics_dia_f64(const mgb_dia* A, double* out14, void* stream);
+int mgb_analytics_dia_f32(const mgb_dia* A, double* out14, void* stream);
+int mgb_analytics_ell(const mgb_ell* A, double* out14, void* stream);
+int mgb_analytics_hyb(const mgb_hyb* A, double* out14, void* stream);
+int mgb_analytics_hdc_f64(const mgb_hdc* A, double* out14, void* stream);
+int mgb_analytics_hdc_f32(const mgb_hdc* A, double* out14, void* stream);
 
 /* Per-row and per-diagonal nonzero counts into device int32 vectors
  * (count_nnz_per_row / count_nnz_per_diagonal,
@@ -249,6 +263,29 @@ int mgb_count_nnz_per_row_csr(const mgb_csr* A, int32_t* out, int init, void* st
 int mgb_count_nnz_per_row_coo(const mgb_coo* A, int32_t* out, int init, void* stream);
 int mgb_count_nnz_per_diagonal_csr(const mgb_csr* A, int32_t* out, int init, void* stream);
 int mgb_count_nnz_per_diagonal_coo(const mgb_coo* A, int32_t* out, int init, void* stream);
+/* The other formats, with the reference's per-format semantics:
+ *   DIA per row: diagonal slots whose column lies inside the matrix, values
+ *     not inspected (impl/Dia/Serial/Morpheus_NonZeros_Per_Row_Impl.hpp:40-72);
+ *     per diagonal: slots holding a nonzero value over all pitch rows
+ *     (impl/Dia/Kokkos/Morpheus_NonZeros_Per_Diagonal_Impl.hpp:37-78).
+ *   ELL per row: slots with a valid column (impl/Ell/Serial/Morpheus_NonZeros_Per_Row_Impl.hpp:40-74);
+ *     per diagonal: with k = the row's valid nonzero slots, the valid nonzero
+ *     slots among its first k slots
+ *     (impl/Ell/Kokkos/Morpheus_NonZeros_Per_Diagonal_Impl.hpp:36-124).
+ *   HYB / HDC: the ELL / DIA part (init as given) plus the COO / CSR part
+ *     (impl/{Hyb,Hdc}/Serial/Morpheus_NonZeros_Per_{Row,Diagonal}_Impl.hpp). */
+int mgb_count_nnz_per_row_dia(const mgb_dia* A, int32_t* out, int init, void* stream);
+int mgb_count_nnz_per_row_ell(const mgb_ell* A, int32_t* out, int init, void* stream);
+int mgb_count_nnz_per_row_hyb(const mgb_hyb* A, int32_t* out, int init, void* stream);
+int mgb_count_nnz_per_row_hdc(const mgb_hdc* A, int32_t* out, int init, void* stream);
+int mgb_count_nnz_per_diagonal_dia_f64(const mgb_dia* A, int32_t* out, int init, void* stream);
+int mgb_count_nnz_per_diagonal_dia_f32(const mgb_dia* A, int32_t* out, int init, void* stream);
+int mgb_count_nnz_per_diagonal_ell_f64(const mgb_ell* A, int32_t* out, int init, void* stream);
+int mgb_count_nnz_per_diagonal_ell_f32(const mgb_ell* A, int32_t* out, int init, void* stream);
+int mgb_count_nnz_per_diagonal_hyb_f64(const mgb_hyb* A, int32_t* out, int init, void* stream);
+int mgb_count_nnz_per_diagonal_hyb_f32(const mgb_hyb* A, int32_t* out, int init, void* stream);
+int mgb_count_nnz_per_diagonal_hdc_f64(const mgb_hdc* A, int32_t* out, int init, void* stream);
+int mgb_count_nnz_per_diagonal_hdc_f32(const mgb_hdc* A, int32_t* out, int init, void* stream);
 /* Number of entries of a device int32 vector that are > threshold and != 0
  * (count_nnz, core/src/Morpheus_VectorAnalytics.hpp:124); with the
  * per-diagonal counts it gives count_diagonals (threshold 0) and
@@ -260,6 +297,15 @@ int mgb_count_nnz_vector(const int32_t* v, int64_t n, int32_t threshold, int64_t
  * (the reference's format choice is the --morpheus-format flag,
  * impl/Morpheus_Core.cpp:101-125). */
 int mgb_features_csr(const mgb_csr* A, float* features12, uint8_t* feasible6, void* stream);
+/* The same features of the other formats, computed in place (see
+ * mgb_analytics_coo): a matrix gets the same features in every format. */
+int mgb_features_coo(const mgb_coo* A, float* features12, uint8_t* feasible6, void* stream);
+int mgb_features_dia_f64(const mgb_dia* A, float* features12, uint8_t* feasible6, void* stream);
+int mgb_features_dia_f32(const mgb_dia* A, float* features12, uint8_t* feasible6, void* stream);
+int mgb_features_ell(const mgb_ell* A, float* features12, uint8_t* feasible6, void* stream);
+int mgb_features_hyb(const mgb_hyb* A, float* features12, uint8_t* feasible6, void* stream);
+int mgb_features_hdc_f64(const mgb_hdc* A, float* features12, uint8_t* feasible6, void* stream);
+int mgb_features_hdc_f32(const mgb_hdc* A, float* features12, uint8_t* feasible6, void* stream);
 
 /* Selector network 12 -> 64 -> 64 -> 6 (ReLU, softmax over feasible formats),
  * FP32 device buffers.  params: mgb_mlp_num_params() floats; mu/sigma: the
@@ -433,6 +479,22 @@ int mgb_cg_csr_f64(const mgb_csr* A, int variant, const double* b, double* x, in
                    int64_t* iters, double* rel_residual, void* stream);
 int mgb_cg_csr_f32(const mgb_csr* A, int variant, const float* b, float* x, int64_t max_iters, double rtol,
                    int64_t* iters, double* rel_residual, void* stream);
+
+/* ---- measurement (no reference counterpart) --------------------------------
+ * Ceilings of the SpMV kernels' non-HBM binding units on the current GPU,
+ * for roofline reports; the caller times the launch (CUDA events on the same
+ * stream).  Blocks of mgb_peak_threads_per_block() threads; `out` receives
+ * one double per thread (blocks * threads entries; keeps the work live).
+ *
+ * FP64 FMA throughput: every thread runs iters x 8 independent fma chains,
+ * so one launch performs blocks * threads * iters * 8 FMA lane-operations. */
+int mgb_peak_dfma_f64(int64_t blocks, int64_t iters, double* out, void* stream);
+/* Random 8-byte gathers from table[table_len] (table_len a power of two; a
+ * table that fits in L2 measures the L2 -> SM sector path the x reads of
+ * scattered SpMV take): blocks * threads * steps * 8 gathers per launch. */
+int mgb_peak_gather_f64(const double* table, int64_t table_len, int64_t blocks, int64_t steps, double* out,
+                        void* stream);
+int mgb_peak_threads_per_block(void);
 
 #ifdef __cplusplus
 } /* extern "C" */

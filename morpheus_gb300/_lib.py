@@ -84,6 +84,14 @@ _SIGS["mgb_count_nnz_per_diagonal_csr"] = (C.c_int, [C.POINTER(Csr), vp, C.c_int
 _SIGS["mgb_count_nnz_per_diagonal_coo"] = (C.c_int, [C.POINTER(Coo), vp, C.c_int, vp])
 _SIGS["mgb_count_nnz_vector"] = (C.c_int, [vp, i64, C.c_int32, C.POINTER(i64), vp])
 _SIGS["mgb_features_csr"] = (C.c_int, [C.POINTER(Csr), C.POINTER(C.c_float), C.POINTER(C.c_uint8), vp])
+for _fmt, _st in (("dia", Dia), ("ell", Ell), ("hyb", Hyb), ("hdc", Hdc)):
+    _SIGS[f"mgb_count_nnz_per_row_{_fmt}"] = (C.c_int, [C.POINTER(_st), vp, C.c_int, vp])
+    for _dt in ("f64", "f32"):
+        _SIGS[f"mgb_count_nnz_per_diagonal_{_fmt}_{_dt}"] = (C.c_int, [C.POINTER(_st), vp, C.c_int, vp])
+for _name, _st in (("coo", Coo), ("dia_f64", Dia), ("dia_f32", Dia), ("ell", Ell), ("hyb", Hyb),
+                   ("hdc_f64", Hdc), ("hdc_f32", Hdc)):
+    _SIGS[f"mgb_analytics_{_name}"] = (C.c_int, [C.POINTER(_st), C.POINTER(C.c_double), vp])
+    _SIGS[f"mgb_features_{_name}"] = (C.c_int, [C.POINTER(_st), C.POINTER(C.c_float), C.POINTER(C.c_uint8), vp])
 _SIGS["mgb_mlp_num_params"] = (C.c_int, [])
 _SIGS["mgb_mlp_forward_f32"] = (C.c_int, [vp, vp, vp, vp, vp, i64, vp, vp])
 _SIGS["mgb_mlp_grad_f32"] = (C.c_int, [vp, vp, vp, vp, vp, vp, i64, vp, vp, vp])
@@ -120,6 +128,9 @@ _SIGS["mgb_convert_coo_to_hdc_plan"] = (C.c_int, [_P(Coo), _P(i64), _P(i64), _P(
 for _dt in ("f64", "f32"):
     _SIGS[f"mgb_coo_sort_by_row_and_column_{_dt}"] = (C.c_int, [_P(Coo), vp])
 _SIGS["mgb_coo_is_sorted"] = (C.c_int, [_P(Coo), _P(C.c_int), vp])
+_SIGS["mgb_peak_dfma_f64"] = (C.c_int, [i64, i64, vp, vp])
+_SIGS["mgb_peak_gather_f64"] = (C.c_int, [vp, i64, i64, i64, vp, vp])
+_SIGS["mgb_peak_threads_per_block"] = (C.c_int, [])
 
 
 def load(path: str | None = None):

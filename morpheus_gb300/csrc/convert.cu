@@ -58,26 +58,42 @@ __global__ void first_bad_col(const int32_t* __restrict__ c, int64_t n, int64_t 
     if (c[i] < 0 || c[i] >= ncols) atomicMin(out, (unsigned long long)i);
 }
 
-// MGB_ERR_INVALID_INPUT if any row is outside [0, nrows) or column outside
-// [0, ncols) (the reference has no check and indexes out of bounds there)
-int validate_coo(const int32_t* rows, const int32_t* cols, int64_t n, int64_t nrows, int64_t ncols,
-                 cudaStream_t s) {
-  if (n <= 0) return MGB_SUCCESS;
-  Scratch sc(s);
-  unsigned long long* d;
-  MGB_SCRATCH(sc, d, 2);
-  const unsigned long long big = ~0ull;
-  MGB_CUDA_CHECK(cudaMemcpyAsync(d, &big, sizeof(big), cudaMemcpyHostToDevice, s));
-  MGB_CUDA_CHECK(cudaMemcpyAsync(d + 1, &big, sizeof(big), cudaMemcpyHostToDevice, s));
-  first_bad_row<<<grid_for(n), 256, 0, s>>>(rows, n, nrows, d);
-  MGB_LAUNCH_CHECK();
-  first_bad_col<<<grid_for(n), 256, 0, s>>>(cols, n, ncols, d + 1);
-  MGB_LAUNCH_CHECK();
-  unsigned long long h[2];
-  MGB_CUDA_CHECK(cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, s));
-  MGB_CUDA_CHECK(cudaStreamSynchronize(s));
-  return (h[0] == big && h[1] == big) ? MGB_SUCCESS : MGB_ERR_INVALID_INPUT;
+// Device words an entry point reads back with one copy and one stream
+// synchronisation: the validation result, the plan's sizes and the
+// sortedness flags, computed by kernels queued one after another.
+struct Words {
+  unsigned long long bad_row, bad_col;  // first index out of range (~0: none)
+  int64_t total, total2;                // plan sizes
+  int32_t sorted, dup, maxv, pad;
+};
+
+int words_alloc(Scratch& sc, Words** d, cudaStream_t s) {
+  MGB_SCRATCH(sc, *d, 1);
+  MGB_CUDA_CHECK(cudaMemsetAsync(*d, 0xff, 2 * sizeof(unsigned long long), s));
+  MGB_CUDA_CHECK(cudaMemsetAsync(&(*d)->total, 0, sizeof(Words) - 2 * sizeof(unsigned long long), s));
+  return MGB_SUCCESS;
 }
+
+int words_read(const Words* d, Words* h, cudaStream_t s) {
+  MGB_CUDA_CHECK(cudaMemcpyAsync(h, d, sizeof(Words), cudaMemcpyDeviceToHost, s));
+  MGB_CUDA_CHECK(cudaStreamSynchronize(s));
+  return MGB_SUCCESS;
+}
+
+// MGB_ERR_INVALID_INPUT (read by the caller with its other words) if any row
+// is outside [0, nrows) or column outside [0, ncols): the reference has no
+// check and indexes out of bounds there.  Queued without a synchronisation.
+int validate_async(const int32_t* rows, const int32_t* cols, int64_t n, int64_t nrows, int64_t ncols, Words* d,
+                   cudaStream_t s) {
+  if (n <= 0) return MGB_SUCCESS;
+  first_bad_row<<<grid_for(n), 256, 0, s>>>(rows, n, nrows, &d->bad_row);
+  MGB_LAUNCH_CHECK();
+  first_bad_col<<<grid_for(n), 256, 0, s>>>(cols, n, ncols, &d->bad_col);
+  MGB_LAUNCH_CHECK();
+  return MGB_SUCCESS;
+}
+
+inline bool words_valid(const Words& h) { return h.bad_row == ~0ull && h.bad_col == ~0ull; }
 
 int sorted_and_dup(const int32_t* r, const int32_t* c, int64_t n, bool* sorted, bool* dup, cudaStream_t s) {
   Scratch sc(s);
@@ -91,10 +107,6 @@ int sorted_and_dup(const int32_t* r, const int32_t* c, int64_t n, bool* sorted, 
   *sorted = h[0] != 0;
   if (dup) *dup = h[1] != 0;
   return MGB_SUCCESS;
-}
-
-int rows_sorted(const int32_t* r, int64_t n, bool* sorted, cudaStream_t s) {
-  return sorted_and_dup(r, nullptr, n, sorted, nullptr, s);
 }
 
 template <typename T>
@@ -183,9 +195,20 @@ int coo_to_csr(const mgb_coo* src, mgb_csr* dst, cudaStream_t s) {
   MGB_REQUIRE(dst->nrows == src->nrows && dst->ncols == src->ncols && dst->nnz == src->nnz, MGB_ERR_INVALID_INPUT);
   MGB_REQUIRE(dst->row_offsets != nullptr, MGB_ERR_BAD_ARGUMENT);
   const int64_t n = src->nnz, N = src->nrows;
-  int st = validate_coo(src->row_indices, src->column_indices, n, N, src->ncols, s);
-  if (st) return st;
   Scratch sc(s);
+  Words* dw;
+  int st = words_alloc(sc, &dw, s);
+  if (st) return st;
+  st = validate_async(src->row_indices, src->column_indices, n, N, src->ncols, dw, s);
+  if (st) return st;
+  if (n > 0) {
+    st = prim::rows_sorted_flag(src->row_indices, n, &dw->sorted, s);
+    if (st) return st;
+  }
+  Words hw;
+  st = words_read(dw, &hw, s);
+  if (st) return st;
+  if (!words_valid(hw)) return MGB_ERR_INVALID_INPUT;
   int32_t* counts;
   MGB_SCRATCH(sc, counts, N + 1);
   st = prim::histogram(src->row_indices, n, counts, N, s);
@@ -193,10 +216,7 @@ int coo_to_csr(const mgb_coo* src, mgb_csr* dst, cudaStream_t s) {
   MGB_CUDA_CHECK(cudaMemsetAsync(counts + N, 0, sizeof(int32_t), s));
   st = prim::exclusive_scan<int32_t, int32_t>(counts, dst->row_offsets, N + 1, s);
   if (st || n == 0) return st;
-  bool sorted = false;
-  st = rows_sorted(src->row_indices, n, &sorted, s);
-  if (st) return st;
-  if (sorted) {
+  if (hw.sorted) {
     MGB_CUDA_CHECK(cudaMemcpyAsync(dst->column_indices, src->column_indices, sizeof(int32_t) * n,
                                    cudaMemcpyDeviceToDevice, s));
     MGB_CUDA_CHECK(cudaMemcpyAsync(dst->values, src->values, sizeof(T) * n, cudaMemcpyDeviceToDevice, s));
@@ -334,47 +354,71 @@ int diag_histogram(const mgb_coo* src, int32_t** bins, int32_t** counts, Scratch
   return prim::histogram(*bins, src->nnz, *counts, nb, s);
 }
 
-int check_coo_src(const mgb_coo* src, cudaStream_t s, bool validate = true) {
+// Argument checks of a COO source (the index range checks are queued with
+// validate_async and read with the caller's other words).
+int check_coo_args(const mgb_coo* src) {
   MGB_REQUIRE(src != nullptr, MGB_ERR_BAD_ARGUMENT);
   MGB_REQUIRE(src->nrows >= 0 && src->ncols >= 0 && src->nnz >= 0, MGB_ERR_BAD_ARGUMENT);
   MGB_REQUIRE(src->nnz == 0 || (src->row_indices && src->column_indices && src->values), MGB_ERR_BAD_ARGUMENT);
   MGB_REQUIRE(src->nrows + src->ncols < INT32_MAX, MGB_ERR_INVALID_INPUT);
-  if (!validate) return MGB_SUCCESS;
-  return validate_coo(src->row_indices, src->column_indices, src->nnz, src->nrows, src->ncols, s);
+  return MGB_SUCCESS;
+}
+
+// COO -> DIA sizes: the diagonal histogram, its occupied bins and their
+// exclusive scan (slot of every occupied diagonal), queued with the
+// validation and, when `flags`, the sortedness flags; one host read.
+struct DiaPlan {
+  int32_t *bins = nullptr, *counts = nullptr, *slot = nullptr;
+  uint8_t* f = nullptr;
+  Words h{};
+};
+int dia_plan(const mgb_coo* src, bool flags, DiaPlan* p, Scratch& sc, cudaStream_t s) {
+  int st = check_coo_args(src);
+  if (st) return st;
+  Words* dw;
+  st = words_alloc(sc, &dw, s);
+  if (st) return st;
+  st = validate_async(src->row_indices, src->column_indices, src->nnz, src->nrows, src->ncols, dw, s);
+  if (st) return st;
+  if (src->nnz > 0) {
+    const int64_t nb = src->nrows + src->ncols - 1;
+    st = diag_histogram(src, &p->bins, &p->counts, sc, s);
+    if (st) return st;
+    MGB_SCRATCH(sc, p->f, nb);
+    MGB_SCRATCH(sc, p->slot, nb);
+    nonzero_flags<<<grid_for(nb), 256, 0, s>>>(p->counts, nb, p->f);
+    MGB_LAUNCH_CHECK();
+    st = prim::exclusive_scan<uint8_t, int32_t>(p->f, p->slot, nb, s, &dw->total);
+    if (st) return st;
+    if (flags) {
+      st = prim::coo_sorted_flags(src->row_indices, src->column_indices, src->nnz, &dw->sorted, &dw->dup, s);
+      if (st) return st;
+    }
+  }
+  st = words_read(dw, &p->h, s);
+  if (st) return st;
+  if (!words_valid(p->h)) return MGB_ERR_INVALID_INPUT;
+  if (exceeds_tolerance(src->nrows, src->nnz, p->h.total)) return MGB_ERR_FORMAT_CONVERSION;
+  return MGB_SUCCESS;
 }
 
 int coo_to_dia_plan(const mgb_coo* src, int64_t* ndiags, cudaStream_t s) {
   MGB_REQUIRE(ndiags != nullptr, MGB_ERR_BAD_ARGUMENT);
-  int st = check_coo_src(src, s);
-  if (st) return st;
   *ndiags = 0;
-  if (src->nnz == 0) return MGB_SUCCESS;
   Scratch sc(s);
-  int32_t *bins, *counts;
-  st = diag_histogram(src, &bins, &counts, sc, s);
-  if (st) return st;
-  const int64_t nb = src->nrows + src->ncols - 1;
-  uint8_t* f;
-  int64_t* d_total;
-  MGB_SCRATCH(sc, f, nb);
-  MGB_SCRATCH(sc, d_total, 1);
-  nonzero_flags<<<grid_for(nb), 256, 0, s>>>(counts, nb, f);
-  MGB_LAUNCH_CHECK();
-  int64_t* pos;
-  MGB_SCRATCH(sc, pos, nb);
-  st = prim::exclusive_scan<uint8_t, int64_t>(f, pos, nb, s, d_total);
-  if (st) return st;
-  st = prim::to_host(d_total, ndiags, s);
-  if (st) return st;
-  if (exceeds_tolerance(src->nrows, src->nnz, *ndiags)) return MGB_ERR_FORMAT_CONVERSION;
-  return MGB_SUCCESS;
+  DiaPlan p;
+  const int st = dia_plan(src, false, &p, sc, s);
+  if (st == MGB_SUCCESS || st == MGB_ERR_FORMAT_CONVERSION) *ndiags = p.h.total;
+  return st;
 }
 
 template <typename T>
 int coo_to_dia(const mgb_coo* src, mgb_dia* dst, cudaStream_t s) {
-  int64_t nd = 0;
-  int st = coo_to_dia_plan(src, &nd, s);
+  Scratch sc(s);
+  DiaPlan p;
+  int st = dia_plan(src, true, &p, sc, s);
   if (st) return st;
+  const int64_t nd = p.h.total;
   MGB_REQUIRE(dst != nullptr, MGB_ERR_BAD_ARGUMENT);
   MGB_REQUIRE(dst->nrows == src->nrows && dst->ncols == src->ncols && dst->nnz == src->nnz && dst->ndiags == nd &&
                   dst->pitch >= src->nrows,
@@ -382,23 +426,11 @@ int coo_to_dia(const mgb_coo* src, mgb_dia* dst, cudaStream_t s) {
   if (nd == 0) return MGB_SUCCESS;
   MGB_REQUIRE(dst->diagonal_offsets && dst->values, MGB_ERR_BAD_ARGUMENT);
   const int64_t n = src->nnz, nb = src->nrows + src->ncols - 1;
-  Scratch sc(s);
-  int32_t *bins, *counts, *slot;
-  st = diag_histogram(src, &bins, &counts, sc, s);
-  if (st) return st;
-  uint8_t* f;
-  MGB_SCRATCH(sc, f, nb);
-  MGB_SCRATCH(sc, slot, nb);
-  nonzero_flags<<<grid_for(nb), 256, 0, s>>>(counts, nb, f);
-  MGB_LAUNCH_CHECK();
-  st = prim::exclusive_scan<uint8_t, int32_t>(f, slot, nb, s);
-  if (st) return st;
-  bins_to_offsets<<<grid_for(nb), 256, 0, s>>>(f, slot, nb, src->nrows, dst->diagonal_offsets);
+  int32_t *bins = p.bins, *slot = p.slot;
+  bins_to_offsets<<<grid_for(nb), 256, 0, s>>>(p.f, slot, nb, src->nrows, dst->diagonal_offsets);
   MGB_LAUNCH_CHECK();
   MGB_CUDA_CHECK(cudaMemsetAsync(dst->values, 0, sizeof(T) * dst->pitch * nd, s));
-  bool sorted = false, dup = true;
-  st = sorted_and_dup(src->row_indices, src->column_indices, n, &sorted, &dup, s);
-  if (st) return st;
+  const bool sorted = p.h.sorted != 0, dup = p.h.dup != 0;
   const T* v = static_cast<const T*>(src->values);
   T* out = static_cast<T*>(dst->values);
   if (sorted && !dup) {
@@ -594,21 +626,19 @@ __global__ void sorted_slots(const int32_t* __restrict__ r, const int32_t* __res
     slot[i] = (int32_t)(i - row_start[r[i]]);
 }
 
-// slots for every entry; *collisions = true when two entries may share a slot
-int compute_slots(const mgb_coo* src, int32_t* slot, bool* collisions, Scratch& sc, cudaStream_t s) {
+// Slot of every entry in its row (the reference's placement counter, which
+// restarts whenever the row changes).  rows_sorted: the rows are
+// non-decreasing (read by the caller); counts: the row histogram (N + 1
+// entries, the last one zero).
+int compute_slots(const mgb_coo* src, bool rows_sorted_flag, int32_t* counts, int32_t* slot, bool* collisions,
+                  Scratch& sc, cudaStream_t s) {
   const int64_t n = src->nnz, N = src->nrows;
   *collisions = false;
   if (n == 0) return MGB_SUCCESS;
-  bool sorted = false;
-  int st = rows_sorted(src->row_indices, n, &sorted, s);
-  if (st) return st;
-  if (sorted) {
-    int32_t *counts, *start;
-    MGB_SCRATCH(sc, counts, N + 1);
+  int st = MGB_SUCCESS;
+  if (rows_sorted_flag) {
+    int32_t* start;
     MGB_SCRATCH(sc, start, N + 1);
-    st = prim::histogram(src->row_indices, n, counts, N, s);
-    if (st) return st;
-    MGB_CUDA_CHECK(cudaMemsetAsync(counts + N, 0, sizeof(int32_t), s));
     st = prim::exclusive_scan<int32_t, int32_t>(counts, start, N + 1, s);
     if (st) return st;
     sorted_slots<<<grid_for(n), 256, 0, s>>>(src->row_indices, start, n, slot);
@@ -700,43 +730,54 @@ int place_ell(const mgb_coo* src, mgb_ell* e, int64_t W, const int32_t* slot, bo
   return MGB_SUCCESS;
 }
 
+// The row histogram of a COO source (N + 1 entries, the last one zero),
+// queued with the validation, the rows-sorted flag and (width > 0) the
+// number of entries a width-W ELL part holds, or (width == 0) the longest
+// row; one host read.
+struct RowPlan {
+  int32_t* counts = nullptr;
+  Words h{};
+};
+int row_plan(const mgb_coo* src, int64_t width, RowPlan* p, Scratch& sc, cudaStream_t s);
+
 int coo_to_ell_plan(const mgb_coo* src, int64_t* epr, cudaStream_t s) {
   MGB_REQUIRE(epr != nullptr, MGB_ERR_BAD_ARGUMENT);
-  int st = check_coo_src(src, s);
-  if (st) return st;
   *epr = 0;
-  if (src->nrows == 0) return MGB_SUCCESS;
+  int st = check_coo_args(src);
+  if (st) return st;
+  if (src->nrows == 0) return src->nnz > 0 ? MGB_ERR_INVALID_INPUT : MGB_SUCCESS;  // every row out of range
   Scratch sc(s);
-  int32_t *counts, *d_max;
-  MGB_SCRATCH(sc, counts, src->nrows);
-  MGB_SCRATCH(sc, d_max, 1);
-  st = prim::histogram(src->row_indices, src->nnz, counts, src->nrows, s);
+  RowPlan p;
+  st = row_plan(src, 0, &p, sc, s);
   if (st) return st;
-  st = prim::reduce_max_i32(counts, src->nrows, d_max, s);
-  if (st) return st;
-  int32_t h = 0;
-  st = prim::to_host(d_max, &h, s);
-  if (st) return st;
-  *epr = h > 0 ? h : 0;
+  *epr = p.h.maxv > 0 ? p.h.maxv : 0;
   if (exceeds_tolerance(src->nrows, src->nnz, *epr)) return MGB_ERR_FORMAT_CONVERSION;
   return MGB_SUCCESS;
 }
 
 template <typename T>
 int coo_to_ell(const mgb_coo* src, mgb_ell* dst, cudaStream_t s) {
-  int64_t W = 0;
-  int st = coo_to_ell_plan(src, &W, s);
+  int st = check_coo_args(src);
   if (st) return st;
+  if (src->nrows == 0 && src->nnz > 0) return MGB_ERR_INVALID_INPUT;  // every row out of range
+  Scratch sc(s);
+  RowPlan p;
+  int64_t W = 0;
+  if (src->nrows > 0) {
+    st = row_plan(src, 0, &p, sc, s);
+    if (st) return st;
+    W = p.h.maxv > 0 ? p.h.maxv : 0;
+    if (exceeds_tolerance(src->nrows, src->nnz, W)) return MGB_ERR_FORMAT_CONVERSION;
+  }
   MGB_REQUIRE(dst != nullptr, MGB_ERR_BAD_ARGUMENT);
   MGB_REQUIRE(dst->nrows == src->nrows && dst->ncols == src->ncols && dst->nnz == src->nnz &&
                   dst->entries_per_row == W && dst->width >= W && dst->pitch >= src->nrows,
               MGB_ERR_INVALID_INPUT);
   MGB_REQUIRE(dst->width * dst->pitch == 0 || (dst->column_indices && dst->values), MGB_ERR_BAD_ARGUMENT);
-  Scratch sc(s);
   int32_t* slot;
   MGB_SCRATCH(sc, slot, src->nnz);
   bool coll = false;
-  st = compute_slots(src, slot, &coll, sc, s);
+  st = compute_slots(src, p.h.sorted != 0, p.counts, slot, &coll, sc, s);
   if (st) return st;
   return place_ell<T>(src, dst, W, slot, coll, nullptr, sc, s);
 }
@@ -752,29 +793,45 @@ __global__ void sum_min_kernel(const int32_t* __restrict__ counts, int64_t n, in
 
 // impl/Hyb/Serial/Morpheus_Convert_Impl.hpp:110-151 (width = max(1, nnz/nrows)
 // unless the caller passes one)
+int row_plan(const mgb_coo* src, int64_t width, RowPlan* p, Scratch& sc, cudaStream_t s) {
+  const int64_t N = src->nrows;
+  Words* dw;
+  int st = words_alloc(sc, &dw, s);
+  if (st) return st;
+  st = validate_async(src->row_indices, src->column_indices, src->nnz, N, src->ncols, dw, s);
+  if (st) return st;
+  MGB_SCRATCH(sc, p->counts, N + 1);
+  st = prim::histogram(src->row_indices, src->nnz, p->counts, N, s);
+  if (st) return st;
+  MGB_CUDA_CHECK(cudaMemsetAsync(p->counts + N, 0, sizeof(int32_t), s));
+  if (width > 0) {
+    sum_min_kernel<<<grid_for(N), 256, 0, s>>>(p->counts, N, width, reinterpret_cast<unsigned long long*>(&dw->total));
+    MGB_LAUNCH_CHECK();
+  } else {
+    st = prim::reduce_max_i32(p->counts, N, &dw->maxv, s);
+    if (st) return st;
+  }
+  st = prim::rows_sorted_flag(src->row_indices, src->nnz, &dw->sorted, s);
+  if (st) return st;
+  st = words_read(dw, &p->h, s);
+  if (st) return st;
+  return words_valid(p->h) ? MGB_SUCCESS : MGB_ERR_INVALID_INPUT;
+}
+
 int coo_to_hyb_plan(const mgb_coo* src, int64_t width, int64_t* epr, int64_t* ell_nnz, int64_t* coo_nnz,
                     cudaStream_t s) {
   MGB_REQUIRE(epr && ell_nnz && coo_nnz && width >= 0, MGB_ERR_BAD_ARGUMENT);
-  int st = check_coo_src(src, s);
+  int st = check_coo_args(src);
   if (st) return st;
   MGB_REQUIRE(src->nrows > 0, MGB_ERR_INVALID_INPUT);  // the reference divides by nrows
   const int64_t W = width > 0 ? width : std::max<int64_t>(1, src->nnz / src->nrows);
   Scratch sc(s);
-  int32_t* counts;
-  unsigned long long* d_sum;
-  MGB_SCRATCH(sc, counts, src->nrows);
-  MGB_SCRATCH(sc, d_sum, 1);
-  st = prim::histogram(src->row_indices, src->nnz, counts, src->nrows, s);
-  if (st) return st;
-  MGB_CUDA_CHECK(cudaMemsetAsync(d_sum, 0, sizeof(unsigned long long), s));
-  sum_min_kernel<<<grid_for(src->nrows), 256, 0, s>>>(counts, src->nrows, W, d_sum);
-  MGB_LAUNCH_CHECK();
-  unsigned long long h = 0;
-  st = prim::to_host(d_sum, &h, s);
+  RowPlan p;
+  st = row_plan(src, W, &p, sc, s);
   if (st) return st;
   *epr = W;
-  *ell_nnz = (int64_t)h;
-  *coo_nnz = src->nnz - (int64_t)h;
+  *ell_nnz = p.h.total;
+  *coo_nnz = src->nnz - p.h.total;
   if (exceeds_tolerance(src->nrows, *ell_nnz, W)) return MGB_ERR_FORMAT_CONVERSION;
   return MGB_SUCCESS;
 }
@@ -782,9 +839,18 @@ int coo_to_hyb_plan(const mgb_coo* src, int64_t width, int64_t* epr, int64_t* el
 template <typename T>
 int coo_to_hyb(const mgb_coo* src, mgb_hyb* dst, cudaStream_t s) {
   MGB_REQUIRE(dst != nullptr, MGB_ERR_BAD_ARGUMENT);
-  int64_t W = 0, en = 0, cn = 0;
-  int st = coo_to_hyb_plan(src, dst->ell.entries_per_row, &W, &en, &cn, s);
+  MGB_REQUIRE(dst->ell.entries_per_row >= 0, MGB_ERR_BAD_ARGUMENT);
+  int st = check_coo_args(src);
   if (st) return st;
+  MGB_REQUIRE(src->nrows > 0, MGB_ERR_INVALID_INPUT);  // the reference divides by nrows
+  const int64_t W = dst->ell.entries_per_row > 0 ? dst->ell.entries_per_row
+                                                 : std::max<int64_t>(1, src->nnz / src->nrows);
+  Scratch sc(s);
+  RowPlan p;
+  st = row_plan(src, W, &p, sc, s);
+  if (st) return st;
+  const int64_t en = p.h.total, cn = src->nnz - p.h.total;
+  if (exceeds_tolerance(src->nrows, en, W)) return MGB_ERR_FORMAT_CONVERSION;
   mgb_ell* e = &dst->ell;
   mgb_coo* c = &dst->coo;
   MGB_REQUIRE(e->nrows == src->nrows && e->ncols == src->ncols && e->nnz == en && e->entries_per_row == W &&
@@ -796,13 +862,12 @@ int coo_to_hyb(const mgb_coo* src, mgb_hyb* dst, cudaStream_t s) {
   const int64_t n = src->nnz;
   st = zero_coo<T>(c, s);
   if (st) return st;
-  Scratch sc(s);
   int32_t* slot;
   uint8_t* to_coo;
   MGB_SCRATCH(sc, slot, n);
   MGB_SCRATCH(sc, to_coo, n);
   bool coll = false;
-  st = compute_slots(src, slot, &coll, sc, s);
+  st = compute_slots(src, p.h.sorted != 0, p.counts, slot, &coll, sc, s);
   if (st) return st;
   st = place_ell<T>(src, e, W, slot, coll, to_coo, sc, s);
   if (st || n == 0) return st;
@@ -893,46 +958,69 @@ __global__ void hdc_dia_place(const int32_t* __restrict__ r, const T* __restrict
   }
 }
 
-int coo_to_hdc_plan(const mgb_coo* src, int64_t* ndiags, int64_t* dia_nnz, int64_t* csr_nnz, cudaStream_t s) {
-  MGB_REQUIRE(ndiags && dia_nnz && csr_nnz, MGB_ERR_BAD_ARGUMENT);
-  int st = check_coo_src(src, s);
+// COO -> HDC sizes: the diagonal histogram, the true diagonals (>= floor(0.2
+// N) entries), their slots and entry count, queued with the validation and
+// (when `flags`) the sortedness flags; one host read.
+struct HdcPlan {
+  int32_t *bins = nullptr, *counts = nullptr, *slot = nullptr;
+  uint8_t* f = nullptr;
+  Words h{};
+};
+int hdc_plan(const mgb_coo* src, bool flags, HdcPlan* p, Scratch& sc, cudaStream_t s) {
+  int st = check_coo_args(src);
   if (st) return st;
   MGB_REQUIRE(src->nrows > 0 && src->ncols > 0, MGB_ERR_INVALID_INPUT);
   const int64_t nb = src->nrows + src->ncols - 1;
   const int32_t min_elem = (int32_t)((double)src->nrows * 0.2);  // HdcMatrix::true_diagonal_ratio
-  Scratch sc(s);
-  int32_t *bins, *counts, *dcounts;
-  st = diag_histogram(src, &bins, &counts, sc, s);
+  Words* dw;
+  st = words_alloc(sc, &dw, s);
   if (st) return st;
-  uint8_t* f;
-  int64_t *d_nd, *d_dn;
-  int64_t* pos;
-  MGB_SCRATCH(sc, f, nb);
+  st = validate_async(src->row_indices, src->column_indices, src->nnz, src->nrows, src->ncols, dw, s);
+  if (st) return st;
+  st = diag_histogram(src, &p->bins, &p->counts, sc, s);
+  if (st) return st;
+  int32_t* dcounts;
+  MGB_SCRATCH(sc, p->f, nb);
   MGB_SCRATCH(sc, dcounts, nb);
-  MGB_SCRATCH(sc, pos, nb);
-  MGB_SCRATCH(sc, d_nd, 1);
-  MGB_SCRATCH(sc, d_dn, 1);
-  true_diag_flags<<<grid_for(nb), 256, 0, s>>>(counts, nb, min_elem, f, dcounts);
+  MGB_SCRATCH(sc, p->slot, nb);
+  true_diag_flags<<<grid_for(nb), 256, 0, s>>>(p->counts, nb, min_elem, p->f, dcounts);
   MGB_LAUNCH_CHECK();
-  st = prim::exclusive_scan<uint8_t, int64_t>(f, pos, nb, s, d_nd);
+  st = prim::exclusive_scan<uint8_t, int32_t>(p->f, p->slot, nb, s, &dw->total);
   if (st) return st;
-  st = prim::reduce_sum_i32(dcounts, nb, d_dn, s);
+  st = prim::reduce_sum_i32(dcounts, nb, &dw->total2, s);
   if (st) return st;
-  st = prim::to_host(d_nd, ndiags, s);
+  if (flags && src->nnz > 0) {
+    st = prim::coo_sorted_flags(src->row_indices, src->column_indices, src->nnz, &dw->sorted, &dw->dup, s);
+    if (st) return st;
+  }
+  st = words_read(dw, &p->h, s);
   if (st) return st;
-  st = prim::to_host(d_dn, dia_nnz, s);
-  if (st) return st;
-  *csr_nnz = src->nnz - *dia_nnz;
-  if (exceeds_tolerance(src->nrows, *dia_nnz, *ndiags)) return MGB_ERR_FORMAT_CONVERSION;
+  if (!words_valid(p->h)) return MGB_ERR_INVALID_INPUT;
+  if (exceeds_tolerance(src->nrows, p->h.total2, p->h.total)) return MGB_ERR_FORMAT_CONVERSION;
   return MGB_SUCCESS;
+}
+
+int coo_to_hdc_plan(const mgb_coo* src, int64_t* ndiags, int64_t* dia_nnz, int64_t* csr_nnz, cudaStream_t s) {
+  MGB_REQUIRE(ndiags && dia_nnz && csr_nnz, MGB_ERR_BAD_ARGUMENT);
+  Scratch sc(s);
+  HdcPlan p;
+  const int st = hdc_plan(src, false, &p, sc, s);
+  if (st == MGB_SUCCESS || st == MGB_ERR_FORMAT_CONVERSION) {
+    *ndiags = p.h.total;
+    *dia_nnz = p.h.total2;
+    *csr_nnz = src->nnz - p.h.total2;
+  }
+  return st;
 }
 
 template <typename T>
 int coo_to_hdc(const mgb_coo* src, mgb_hdc* dst, cudaStream_t s) {
   MGB_REQUIRE(dst != nullptr, MGB_ERR_BAD_ARGUMENT);
-  int64_t nd = 0, dn = 0, cn = 0;
-  int st = coo_to_hdc_plan(src, &nd, &dn, &cn, s);
+  Scratch sc(s);
+  HdcPlan p;
+  int st = hdc_plan(src, true, &p, sc, s);
   if (st) return st;
+  const int64_t nd = p.h.total, dn = p.h.total2, cn = src->nnz - p.h.total2;
   mgb_dia* D = &dst->dia;
   mgb_csr* C = &dst->csr;
   MGB_REQUIRE(D->nrows == src->nrows && D->ncols == src->ncols && D->nnz == dn && D->ndiags == nd &&
@@ -942,19 +1030,8 @@ int coo_to_hdc(const mgb_coo* src, mgb_hdc* dst, cudaStream_t s) {
   MGB_REQUIRE(C->row_offsets && (nd == 0 || (D->diagonal_offsets && D->values)), MGB_ERR_BAD_ARGUMENT);
   MGB_REQUIRE(cn == 0 || (C->column_indices && C->values), MGB_ERR_BAD_ARGUMENT);
   const int64_t n = src->nnz, N = src->nrows, nb = src->nrows + src->ncols - 1;
-  const int32_t min_elem = (int32_t)((double)src->nrows * 0.2);
-  Scratch sc(s);
-  int32_t *bins, *counts, *dcounts, *slot;
-  st = diag_histogram(src, &bins, &counts, sc, s);
-  if (st) return st;
-  uint8_t* f;
-  MGB_SCRATCH(sc, f, nb);
-  MGB_SCRATCH(sc, dcounts, nb);
-  MGB_SCRATCH(sc, slot, nb);
-  true_diag_flags<<<grid_for(nb), 256, 0, s>>>(counts, nb, min_elem, f, dcounts);
-  MGB_LAUNCH_CHECK();
-  st = prim::exclusive_scan<uint8_t, int32_t>(f, slot, nb, s);
-  if (st) return st;
+  uint8_t* f = p.f;
+  int32_t* slot = p.slot;
   if (nd > 0) {
     hdc_offsets<<<grid_for(nb), 256, 0, s>>>(f, slot, nb, N, D->diagonal_offsets);
     MGB_LAUNCH_CHECK();
@@ -982,16 +1059,11 @@ int coo_to_hdc(const mgb_coo* src, mgb_hdc* dst, cudaStream_t s) {
   MGB_LAUNCH_CHECK();
   st = prim::exclusive_scan<uint8_t, int64_t>(is_csr, cpos, n, s, d_csr);
   if (st) return st;
-  int64_t ncsr = 0;
-  st = prim::to_host(d_csr, &ncsr, s);
-  if (st) return st;
   // a non-square matrix with a true diagonal in the midpoint bin sends more
-  // entries to CSR than were counted (the reference writes out of bounds)
-  MGB_REQUIRE(ncsr <= cn, MGB_ERR_RUNTIME);
+  // entries to CSR than were counted (the reference writes out of bounds):
+  // the scatter below stops at cn, and the count is checked at the end
   const T* v = static_cast<const T*>(src->values);
-  bool sorted = false, dup = true;
-  st = sorted_and_dup(src->row_indices, src->column_indices, n, &sorted, &dup, s);
-  if (st) return st;
+  const bool sorted = p.h.sorted != 0, dup = p.h.dup != 0;
   if (nd > 0) {
     if (sorted && !dup) {
       hdc_dia_place<T><<<grid_for(n), 256, 0, s>>>(src->row_indices, v, dslot, n, D->pitch, static_cast<T*>(D->values),
@@ -1017,18 +1089,24 @@ int coo_to_hdc(const mgb_coo* src, mgb_hdc* dst, cudaStream_t s) {
   if (cn > 0) {
     MGB_CUDA_CHECK(cudaMemsetAsync(C->column_indices, 0, sizeof(int32_t) * cn, s));
     MGB_CUDA_CHECK(cudaMemsetAsync(C->values, 0, sizeof(T) * cn, s));
+    // slots the scatter leaves empty hold row N, which the histogram ignores
+    st = fill<int32_t>(rows_c, (int32_t)N, cn, s);
+    if (st) return st;
     coo_part_scatter<T><<<grid_for(n), 256, 0, s>>>(src->row_indices, src->column_indices, v, is_csr, cpos, n, cn,
                                                     rows_c, C->column_indices, static_cast<T*>(C->values));
     MGB_LAUNCH_CHECK();
   }
-  st = prim::histogram(rows_c, ncsr, counts_c, N, s);
+  st = prim::histogram(rows_c, cn, counts_c, N, s);
   if (st) return st;
   MGB_CUDA_CHECK(cudaMemsetAsync(counts_c + N, 0, sizeof(int32_t), s));
   st = prim::exclusive_scan<int32_t, int32_t>(counts_c, C->row_offsets, N + 1, s);
   if (st) return st;
   const int32_t last = (int32_t)cn;
+  int64_t ncsr = 0;
   MGB_CUDA_CHECK(cudaMemcpyAsync(C->row_offsets + N, &last, sizeof(int32_t), cudaMemcpyHostToDevice, s));
-  MGB_CUDA_CHECK(cudaStreamSynchronize(s));  // 'last' lives on this stack frame
+  MGB_CUDA_CHECK(cudaMemcpyAsync(&ncsr, d_csr, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  MGB_CUDA_CHECK(cudaStreamSynchronize(s));  // 'last' and 'ncsr' live on this stack frame
+  MGB_REQUIRE(ncsr <= cn, MGB_ERR_RUNTIME);
   return MGB_SUCCESS;
 }
 
@@ -1039,18 +1117,20 @@ int coo_sort(mgb_coo* A, cudaStream_t s) {
   if (A->nnz <= 1) return MGB_SUCCESS;
   MGB_REQUIRE(A->row_indices && A->column_indices && A->values, MGB_ERR_BAD_ARGUMENT);
   Scratch sc(s);
-  int32_t* d_max;
-  MGB_SCRATCH(sc, d_max, 1);
-  int st = prim::reduce_max_i32(A->row_indices, A->nnz, d_max, s);
+  Words* dw;
+  int st = words_alloc(sc, &dw, s);
   if (st) return st;
-  int32_t maxr = 0;
-  st = prim::to_host(d_max, &maxr, s);
+  st = prim::reduce_max_i32(A->row_indices, A->nnz, &dw->maxv, s);
   if (st) return st;
   // rows and columns must be >= 0 (the counting sort indexes by them)
-  st = validate_coo(A->row_indices, A->column_indices, A->nnz, (int64_t)maxr + 1, INT32_MAX, s);
+  st = validate_async(A->row_indices, A->column_indices, A->nnz, INT32_MAX, INT32_MAX, dw, s);
   if (st) return st;
+  Words hw;
+  st = words_read(dw, &hw, s);
+  if (st) return st;
+  if (!words_valid(hw)) return MGB_ERR_INVALID_INPUT;
   return sort_coo_inplace<T>(A->row_indices, A->column_indices, static_cast<T*>(A->values), A->nnz,
-                             (int64_t)maxr + 1, s);
+                             (int64_t)hw.maxv + 1, s);
 }
 
 int coo_is_sorted(const mgb_coo* A, int* out, cudaStream_t s) {

@@ -10,10 +10,13 @@
 // with init, then the COO part accumulating into y.
 //
 // Layout: slot (i, n) at [i + pitch * n], pitch = nrows (column-major, the
-// reference's CUDA LayoutLeft).  A thread owns RPT consecutive rows and reads
-// each slot column with one 16-byte vector load of column indices and, only
-// where a slot holds an entry, the values (padding values are never read:
-// a warp whose 32*RPT rows are all padding at slot n skips the value sector).
+// reference's CUDA LayoutLeft).  A thread owns RPT = 4 consecutive rows and
+// reads each slot column with one 16-byte load of their column indices
+// (int4) and, only where one of the 4 slots holds an entry, 16-byte loads of
+// the values (two double2 / one float4): padding values are never read, and
+// a warp whose 128 rows are all padding at slot n skips the value sectors.
+// Pitches or pointers that do not allow 16-byte loads take 2 or 1 rows per
+// thread.
 #include "mgb_internal.cuh"
 
 namespace mgb {
@@ -22,6 +25,18 @@ namespace {
 constexpr int ELL_THREADS = 256;
 
 template <typename T, int RPT> struct EllVec;
+template <> struct EllVec<double, 4> {
+  static __device__ __forceinline__ void load(const double* p, double* o) {
+    const double2 a = __ldcs(reinterpret_cast<const double2*>(p));
+    const double2 b = __ldcs(reinterpret_cast<const double2*>(p) + 1);
+    o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y;
+  }
+};
+template <> struct EllVec<float, 4> {
+  static __device__ __forceinline__ void load(const float* p, float* o) {
+    const float4 v = __ldcs(reinterpret_cast<const float4*>(p)); o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+  }
+};
 template <> struct EllVec<double, 2> {
   static __device__ __forceinline__ void load(const double* p, double* o) {
     const double2 v = __ldcs(reinterpret_cast<const double2*>(p)); o[0] = v.x; o[1] = v.y;
@@ -37,6 +52,11 @@ template <typename T> struct EllVec<T, 1> {
 };
 
 template <int RPT> struct IdxVec;
+template <> struct IdxVec<4> {
+  static __device__ __forceinline__ void load(const int32_t* p, int32_t* o) {
+    const int4 v = __ldcs(reinterpret_cast<const int4*>(p)); o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+  }
+};
 template <> struct IdxVec<2> {
   static __device__ __forceinline__ void load(const int32_t* p, int32_t* o) {
     const int2 v = __ldcs(reinterpret_cast<const int2*>(p)); o[0] = v.x; o[1] = v.y;
@@ -100,16 +120,21 @@ int launch_ell(const mgb_ell* A, const T* x, T* y, int init, cudaStream_t s) {
   MGB_REQUIRE(y != nullptr, MGB_ERR_BAD_ARGUMENT);
   MGB_REQUIRE(A->width == 0 || (A->pitch >= A->nrows && A->column_indices && A->values && x),
               MGB_ERR_BAD_ARGUMENT);
-  const bool vec_ok = (A->pitch % 2 == 0) &&
-                      (reinterpret_cast<uintptr_t>(A->values) % (2 * sizeof(T)) == 0) &&
-                      (reinterpret_cast<uintptr_t>(A->column_indices) % 8 == 0);
-  const int rpt = vec_ok ? 2 : 1;
+  // 16-byte loads need every slot column (row0 + pitch * n, row0 a multiple
+  // of RPT) 16-byte aligned: pitch a multiple of 4 and 16-byte base pointers
+  const uintptr_t ap = reinterpret_cast<uintptr_t>(A->values), ai = reinterpret_cast<uintptr_t>(A->column_indices);
+  const bool vec4 = (A->pitch % 4 == 0) && (ap % 16 == 0) && (ai % 16 == 0);
+  const bool vec2 = (A->pitch % 2 == 0) && (ap % (2 * sizeof(T)) == 0) && (ai % 8 == 0);
+  const int rpt = vec4 ? 4 : (vec2 ? 2 : 1);
   const int64_t groups = (A->nrows + rpt - 1) / rpt;
   int64_t blocks = (groups + ELL_THREADS - 1) / ELL_THREADS;
   const int64_t cap = (int64_t)num_sms() * 64;
   if (blocks > cap) blocks = cap;
   const T* va = static_cast<const T*>(A->values);
-  if (vec_ok)
+  if (vec4)
+    spmv_ell_rows<T, 4><<<(unsigned)blocks, ELL_THREADS, 0, s>>>(
+        A->nrows, A->ncols, A->width, A->pitch, A->column_indices, va, x, y, init);
+  else if (vec2)
     spmv_ell_rows<T, 2><<<(unsigned)blocks, ELL_THREADS, 0, s>>>(
         A->nrows, A->ncols, A->width, A->pitch, A->column_indices, va, x, y, init);
   else

@@ -268,6 +268,121 @@ void count_nnz_per_diagonal(const Coo<T>& A, std::vector<idx_t>& out,
   }
 }
 
+// core/src/impl/Csr/Kokkos/Morpheus_NonZeros_Per_Diagonal_Impl.hpp:38-78
+template <class T>
+void count_nnz_per_diagonal(const Csr<T>& A, std::vector<idx_t>& out,
+                            bool init) {
+  if (init) std::fill(out.begin(), out.end(), 0);
+  for (sz_t i = 0; i < A.nrows; i++)
+    for (idx_t jj = A.row_offsets[i]; jj < A.row_offsets[i + 1]; jj++)
+      out[(sz_t)((int64_t)A.column_indices[jj] - (int64_t)i +
+                 (int64_t)A.nrows - 1)]++;
+}
+
+// core/src/impl/Dia/Kokkos/Morpheus_NonZeros_Per_Diagonal_Impl.hpp:37-78:
+// nonzero slots of each diagonal, over all pitch rows of the slab
+template <class T>
+void count_nnz_per_diagonal(const Dia<T>& A, std::vector<idx_t>& out,
+                            bool init) {
+  if (init) std::fill(out.begin(), out.end(), 0);
+  for (sz_t i = 0; i < A.ndiags; i++) {
+    const sz_t idx = (sz_t)((int64_t)A.diagonal_offsets[i] + (int64_t)A.nrows - 1);
+    for (sz_t j = 0; j < A.pitch; j++)
+      if (A.v(j, i) != T(0)) out[idx] += 1;
+  }
+}
+
+// core/src/impl/Ell/Kokkos/Morpheus_NonZeros_Per_Diagonal_Impl.hpp:36-124:
+// k = slots of row i with a valid column and a nonzero value; then the first
+// k slots of the row are scanned and the valid nonzero ones counted
+template <class T>
+void count_nnz_per_diagonal(const Ell<T>& A, std::vector<idx_t>& out,
+                            bool init) {
+  if (init) std::fill(out.begin(), out.end(), 0);
+  for (sz_t i = 0; i < A.nrows; i++) {
+    sz_t k = 0;
+    for (sz_t n = 0; n < A.width; n++)
+      if (A.ci(i, n) != Ell<T>::invalid_index && A.v(i, n) != T(0)) k += 1;
+    for (sz_t n = 0; n < k; n++) {
+      const idx_t col = A.ci(i, n);
+      if (col != Ell<T>::invalid_index && A.v(i, n) != T(0))
+        out[(sz_t)((int64_t)col - (int64_t)i + (int64_t)A.nrows - 1)]++;
+    }
+  }
+}
+
+// core/src/impl/Hyb/Serial/Morpheus_NonZeros_Per_Diagonal_Impl.hpp:43-59
+template <class T>
+void count_nnz_per_diagonal(const Hyb<T>& A, std::vector<idx_t>& out,
+                            bool init) {
+  count_nnz_per_diagonal(A.ell, out, init);
+  count_nnz_per_diagonal(A.coo, out, false);
+}
+
+// core/src/impl/Hdc/Serial/Morpheus_NonZeros_Per_Diagonal_Impl.hpp:42-58
+template <class T>
+void count_nnz_per_diagonal(const Hdc<T>& A, std::vector<idx_t>& out,
+                            bool init) {
+  count_nnz_per_diagonal(A.dia, out, init);
+  count_nnz_per_diagonal(A.csr, out, false);
+}
+
+// core/src/impl/Coo/Serial/Morpheus_NonZeros_Per_Row_Impl.hpp:41-67
+template <class T>
+void count_nnz_per_row(const Coo<T>& A, std::vector<idx_t>& out, bool init) {
+  if (init)
+    for (sz_t n = 0; n < A.nrows; n++) out[n] = 0;
+  for (sz_t n = 0; n < A.nnz; n++) out[(sz_t)A.row_indices[n]]++;
+}
+
+// core/src/impl/Csr/Serial/Morpheus_NonZeros_Per_Row_Impl.hpp:40-65
+template <class T>
+void count_nnz_per_row(const Csr<T>& A, std::vector<idx_t>& out, bool init) {
+  for (sz_t i = 0; i < A.nrows; i++) {
+    idx_t non_zeros = init ? 0 : out[i];
+    for (idx_t jj = A.row_offsets[i]; jj < A.row_offsets[i + 1]; jj++) non_zeros++;
+    out[i] = non_zeros;
+  }
+}
+
+// core/src/impl/Dia/Serial/Morpheus_NonZeros_Per_Row_Impl.hpp:40-72:
+// diagonal slots whose column lies inside the matrix (values not inspected)
+template <class T>
+void count_nnz_per_row(const Dia<T>& A, std::vector<idx_t>& out, bool init) {
+  for (sz_t row = 0; row < A.nrows; row++) {
+    idx_t non_zeros = init ? 0 : out[row];
+    for (sz_t n = 0; n < A.ndiags; n++) {
+      const int64_t col = (int64_t)row + A.diagonal_offsets[n];
+      if (col >= 0 && col < (int64_t)A.ncols) non_zeros++;
+    }
+    out[row] = non_zeros;
+  }
+}
+
+// core/src/impl/Ell/Serial/Morpheus_NonZeros_Per_Row_Impl.hpp:40-74
+template <class T>
+void count_nnz_per_row(const Ell<T>& A, std::vector<idx_t>& out, bool init) {
+  if (init)
+    for (sz_t n = 0; n < A.nrows; n++) out[n] = 0;
+  for (sz_t i = 0; i < A.nrows; i++)
+    for (sz_t n = 0; n < A.width; n++)
+      if (A.ci(i, n) != Ell<T>::invalid_index) out[i]++;
+}
+
+// core/src/impl/Hyb/Serial/Morpheus_NonZeros_Per_Row_Impl.hpp:42-58
+template <class T>
+void count_nnz_per_row(const Hyb<T>& A, std::vector<idx_t>& out, bool init) {
+  count_nnz_per_row(A.ell, out, init);
+  count_nnz_per_row(A.coo, out, false);
+}
+
+// core/src/impl/Hdc/Serial/Morpheus_NonZeros_Per_Row_Impl.hpp:42-58
+template <class T>
+void count_nnz_per_row(const Hdc<T>& A, std::vector<idx_t>& out, bool init) {
+  count_nnz_per_row(A.dia, out, init);
+  count_nnz_per_row(A.csr, out, false);
+}
+
 // ---------------------------------------------------------------------------
 // Conversions (Serial).  Every pair goes through COO like the reference's
 // generic hub core/src/impl/Morpheus_Convert_Impl.hpp:82-104.
@@ -1129,14 +1244,32 @@ int orc_is_sorted(void* p) {
   return is_sorted(std::get<Coo<float>>(h->f)) ? 1 : 0;
 }
 
-int orc_count_nnz_per_diagonal(void* p, int32_t* out) {
+// count_nnz_per_diagonal / count_nnz_per_row of the active container
+// (core/src/Morpheus_MatrixAnalytics.hpp:112-124, 206-218), each format by
+// its own rule above; init == 0 adds to out's current contents.
+int orc_count_nnz_per_diagonal(void* p, int32_t* out, int init) {
   Handle* h = static_cast<Handle*>(p);
   return guarded([&] {
     with_dyn(h, [&](auto& d) {
-      auto& m = std::get<0>(d);
-      std::vector<idx_t> v(m.nrows + m.ncols - 1, 0);
-      count_nnz_per_diagonal(m, v, true);
-      std::memcpy(out, v.data(), v.size() * sizeof(idx_t));
+      std::visit([&](const auto& m) {
+        std::vector<idx_t> v(out, out + (m.nrows + m.ncols - 1));
+        count_nnz_per_diagonal(m, v, init != 0);
+        std::memcpy(out, v.data(), v.size() * sizeof(idx_t));
+      }, d);
+      return 0;
+    });
+  });
+}
+
+int orc_count_nnz_per_row(void* p, int32_t* out, int init) {
+  Handle* h = static_cast<Handle*>(p);
+  return guarded([&] {
+    with_dyn(h, [&](auto& d) {
+      std::visit([&](const auto& m) {
+        std::vector<idx_t> v(out, out + m.nrows);
+        count_nnz_per_row(m, v, init != 0);
+        std::memcpy(out, v.data(), v.size() * sizeof(idx_t));
+      }, d);
       return 0;
     });
   });

@@ -68,7 +68,8 @@ def lib():
         L.orc_convert_inplace.argtypes = [C.c_void_p, C.c_int]
         L.orc_sort_by_row_and_column.argtypes = [C.c_void_p]
         L.orc_is_sorted.argtypes = [C.c_void_p]
-        L.orc_count_nnz_per_diagonal.argtypes = [C.c_void_p, C.c_void_p]
+        L.orc_count_nnz_per_diagonal.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
+        L.orc_count_nnz_per_row.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
         L.orc_multiply.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int]
         L.orc_dot_f64.restype = C.c_double
         L.orc_dot_f64.argtypes = [C.c_int64, C.c_void_p, C.c_void_p]
@@ -254,12 +255,24 @@ class OracleMatrix:
     def is_sorted(self) -> bool:
         return bool(lib().orc_is_sorted(self.h))
 
-    def count_nnz_per_diagonal(self) -> np.ndarray:
+    def count_nnz_per_diagonal(self, out: np.ndarray | None = None, init: bool = True) -> np.ndarray:
+        """The reference's count_nnz_per_diagonal of this container's format."""
         s = self.shape()
-        out = np.zeros(s[1] + s[2] - 1, dtype=np.int32)
-        st = lib().orc_count_nnz_per_diagonal(self.h, _ptr(out))
+        out = np.zeros(s[1] + s[2] - 1, dtype=np.int32) if out is None else out
+        assert out.dtype == np.int32 and out.size == s[1] + s[2] - 1 and out.flags.c_contiguous
+        st = lib().orc_count_nnz_per_diagonal(self.h, _ptr(out), 1 if init else 0)
         if st != STATUS_OK:
             raise OracleError(st, "count_nnz_per_diagonal")
+        return out
+
+    def count_nnz_per_row(self, out: np.ndarray | None = None, init: bool = True) -> np.ndarray:
+        """The reference's count_nnz_per_row of this container's format."""
+        s = self.shape()
+        out = np.zeros(s[1], dtype=np.int32) if out is None else out
+        assert out.dtype == np.int32 and out.size == s[1] and out.flags.c_contiguous
+        st = lib().orc_count_nnz_per_row(self.h, _ptr(out), 1 if init else 0)
+        if st != STATUS_OK:
+            raise OracleError(st, "count_nnz_per_row")
         return out
 
     def multiply(self, x: np.ndarray, y: np.ndarray | None = None, init: bool = True,

@@ -243,3 +243,90 @@ def test_generator_sizes():
     starts = np.zeros(A["nnz"], bool)
     starts[ro[:-1][lens > 0]] = True
     assert np.all(d[~starts[1:]] > 0)
+
+
+def _numpy_counts(hm: dict):
+    """Independent per-format counts (the reference's rules, in numpy)."""
+    f, N, M = hm["format"], hm["nrows"], hm["ncols"]
+    rows = np.zeros(N, dtype=np.int64)
+    diag = np.zeros(N + M - 1, dtype=np.int64)
+    if f == 0:
+        np.add.at(rows, hm["row_indices"], 1)
+        np.add.at(diag, hm["column_indices"] - hm["row_indices"] + N - 1, 1)
+    elif f == 1:
+        lens = np.diff(hm["row_offsets"])
+        rows += lens
+        r = np.repeat(np.arange(N), lens)
+        np.add.at(diag, hm["column_indices"] - r + N - 1, 1)
+    elif f == 2:
+        P, off = hm["pitch"], hm["diagonal_offsets"]
+        v = hm["values"].reshape(hm["ndiags"], P)
+        for k, o in enumerate(off):
+            c = np.arange(N) + o
+            rows += (c >= 0) & (c < M)
+            diag[o + N - 1] += np.count_nonzero(v[k])
+    elif f == 3:
+        W, P = hm["width"], hm["pitch"]
+        ci = hm["column_indices"].reshape(W, P)[:, :N].T
+        v = hm["values"].reshape(W, P)[:, :N].T
+        valid = ci != -1
+        rows += valid.sum(1)
+        good = valid & (v != 0)
+        k = good.sum(1)
+        for i in range(N):
+            for n in range(k[i]):
+                if good[i, n]:
+                    diag[ci[i, n] - i + N - 1] += 1
+    else:
+        a, b = (hm["ell"], hm["coo"]) if f == 4 else (hm["dia"], hm["csr"])
+        ra, da = _numpy_counts(a)
+        rb, db = _numpy_counts(b)
+        rows, diag = ra + rb, da + db
+    return rows, diag
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
+@pytest.mark.parametrize("fmt", FORMATS)
+def test_counts_per_format_golden(fmt, dtype):
+    """count_nnz_per_row / count_nnz_per_diagonal of every golden container
+    by the format's own rule (impl/<Fmt>/Serial/Morpheus_NonZeros_Per_Row_Impl.hpp,
+    impl/<Fmt>/{Kokkos,Serial}/Morpheus_NonZeros_Per_Diagonal_Impl.hpp),
+    against an independent numpy restatement; init=False accumulates."""
+    hm = golden(dtype)[fmt]
+    om = O.OracleMatrix.from_host(hm)
+    rows, diag = _numpy_counts(hm)
+    assert np.array_equal(om.count_nnz_per_row(), rows)
+    assert np.array_equal(om.count_nnz_per_diagonal(), diag)
+    r2 = om.count_nnz_per_row()
+    om.count_nnz_per_row(out=r2, init=False)
+    assert np.array_equal(r2, 2 * rows)
+    d2 = om.count_nnz_per_diagonal()
+    om.count_nnz_per_diagonal(out=d2, init=False)
+    assert np.array_equal(d2, 2 * diag)
+    # the golden matrix stores no explicit zeros: every format counts its 32 entries
+    assert diag.sum() == 32 and (fmt == "DIA" or fmt == "HDC" or rows.sum() == 32)
+
+
+def test_counts_format_quirks():
+    """DIA rows count in-range diagonal slots, explicit zeros included; an ELL
+    row whose valid nonzero slots do not come first loses the later ones in
+    the per-diagonal count (the reference's scan of the first k slots)."""
+    dia = {"format": 2, "nrows": 4, "ncols": 4, "nnz": 5, "ndiags": 2, "pitch": 32, "alignment": 32,
+           "diagonal_offsets": np.array([0, 1], np.int32), "values": np.zeros(64)}
+    dia["values"][[0, 1, 2, 3]] = [1.0, 0.0, 3.0, 4.0]  # main diagonal, an explicit zero in row 1
+    dia["values"][32 + 0] = 5.0                        # (0, 1)
+    om = O.OracleMatrix.from_host(dia)
+    assert om.count_nnz_per_row().tolist() == [2, 2, 2, 1]
+    d = om.count_nnz_per_diagonal()
+    assert d[3] == 3 and d[4] == 1 and d.sum() == 4
+    ell = {"format": 3, "nrows": 2, "ncols": 5, "nnz": 4, "entries_per_row": 3, "width": 32, "pitch": 2,
+           "alignment": 32, "column_indices": np.full(64, -1, np.int32), "values": np.zeros(64)}
+    ell["column_indices"][[0, 4]] = [0, 3]   # row 0: slot 0 -> col 0, slot 2 -> col 3 (slot 1 a gap)
+    ell["values"][[0, 4]] = [1.0, 2.0]
+    ell["column_indices"][[1, 3]] = [1, 2]   # row 1: slot 0 -> col 1 holding 0.0, slot 1 -> col 2
+    ell["values"][[1, 3]] = [0.0, 7.0]
+    om = O.OracleMatrix.from_host(ell)
+    assert om.count_nnz_per_row().tolist() == [2, 2]
+    d = om.count_nnz_per_diagonal()
+    # row 0: k = 2, slots 0..1 -> only (0, 0); row 1: k = 1, slot 0 holds a zero -> nothing
+    assert d.tolist() == [0, 1, 0, 0, 0, 0]

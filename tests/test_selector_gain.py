@@ -14,12 +14,11 @@ exhaustive best time on average (mean regret), capture at least 90 % of the
 exhaustive oracle's (log) speed-up over CSR only, and beat the rule-based
 selector whose thresholds are tuned on the same training matrices.  The
 absolute speed-up over CSR only is bounded by the oracle's, which shrinks as
-the CSR kernels get faster: with the chunk-planned lane-segment kernel and
-the reworked row-tile kernels the best format is 1.23x faster than CSR on
-this corpus in geometric mean (1.42x with the earlier CSR kernels, 1.64x
-before the adaptive chunk size), so the absolute bar is 1.15x.  The CPU test
-runs the network through the FP64 oracle; the GPU test through the
-library's forward kernel.
+the CSR kernels get faster: on this corpus (matrices up to 120 M entries, a
+quarter of them without off-pattern entries) the best format is 1.28x faster
+than CSR in geometric mean and the network reaches 1.25x, so the absolute
+bar is 1.15x.  The CPU test runs the network through the FP64 oracle; the
+GPU test through the library's forward kernel.
 """
 import os
 
