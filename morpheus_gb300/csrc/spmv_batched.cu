@@ -35,14 +35,21 @@ namespace mgb {
 namespace {
 
 constexpr int BAT_WARPS = 8;
-constexpr int BAT_NCONFIGS = 10;
-constexpr int BAT_FIRST_XS = 6;  // configurations 6, 7 keep x in shared memory
-constexpr int BAT_FIRST_XL1 = 8;  // configurations 8, 9: matrix per CTA, x through L1
+constexpr int BAT_NCONFIGS = 11;
+constexpr int BAT_FIRST_XS = 6;  // configurations >= 6 are matrix per CTA (largest first)
+// configurations 6, 7 and 10 keep x in shared memory, 8 and 9 read it through L1
+constexpr bool bat_is_xl1(int c) { return c == 8 || c == 9; }
 // chunk-queue configs: nonzeros per chunk; matrix-per-CTA configs: 0 (each
-// matrix is cut into 8 x BAT_XS_CPW chunks of at least 256 nonzeros)
-constexpr int64_t BAT_CHUNK[BAT_NCONFIGS] = {512, 1024, 2048, 4096, 1024, 2048, 0, 0, 0, 0};
-constexpr int BAT_SEG[BAT_NCONFIGS] = {8, 8, 8, 8, 4, 4, 8, 8, 8, 8};
-constexpr int BAT_XS_CPW[BAT_NCONFIGS] = {0, 0, 0, 0, 0, 0, 1, 2, 1, 2};  // chunks per warp
+// matrix is cut into WARPS x BAT_XS_CPW chunks of at least 256 nonzeros)
+constexpr int64_t BAT_CHUNK[BAT_NCONFIGS] = {512, 1024, 2048, 4096, 1024, 2048, 0, 0, 0, 0, 0};
+constexpr int BAT_SEG[BAT_NCONFIGS] = {8, 8, 8, 8, 4, 4, 8, 8, 8, 8, 8};
+constexpr int BAT_XS_CPW[BAT_NCONFIGS] = {0, 0, 0, 0, 0, 0, 1, 2, 1, 2, 2};  // chunks per warp
+// x-in-shared-memory configs: x buffers and warps per CTA (6: two CTAs of 8
+// warps per SM; 7: one CTA of 16 warps, the next matrix's x copied during
+// this one; 10: one CTA of 24 warps, 32-bit chunk indices)
+constexpr int bat_xs_nbuf(int c) { return c == 7 ? 2 : 1; }
+constexpr int bat_xs_warps(int c) { return c == 6 ? 8 : (c == 7 ? 16 : 24); }
+constexpr int bat_xs_ctas(int c) { return bat_xs_warps(c) >= 16 ? 1 : 16 / bat_xs_warps(c); }
 constexpr int BAT_XS_BYTES = 64 * 1024;  // per x buffer (larger x: read from global)
 // workspace: int32 header[4] = {work counter, total work items, planned
 // config, error flag}, then int32[nitems + 1]: the chunk prefix (chunk-queue
@@ -122,18 +129,21 @@ __device__ __forceinline__ void copy_x_async(T* xs, const T* __restrict__ xg, in
                  : "memory");
 }
 
-// One CTA per matrix at a time, x in shared memory (configs >= BAT_FIRST_XS).
+// One CTA per matrix at a time, x in shared memory (configs 6, 7, 10).
 // Each CTA takes the next matrix (largest first), copies its x (up to
 // BAT_XS_BYTES) into shared memory with cp.async, and its warps split the
 // matrix into nnz-balanced chunks whose random x reads are shared-memory
 // reads.  With NBUF = 2 the copy of the next matrix's x is in flight while
 // the CTA works on the current one (one CTA of 16 warps per SM); with NBUF =
-// 1 two CTAs of 8 warps share an SM, and one computes while the other
-// copies.  A wider x is read from global memory.  No thread waits on another
-// CTA, so there is no spin-wait.
+// 1 and 8 warps two CTAs share an SM, and one computes while the other
+// copies; with 24 warps one CTA holds as many warps as the chunk queue (its
+// chunks then use 32-bit indices and skip items beyond them, as the chunk
+// queue does).  A wider x is read from global memory.  No thread waits on
+// another CTA, so there is no spin-wait.
 template <typename T, int CFG, int NBUF, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32, 16 / WARPS)
+__global__ void __launch_bounds__(WARPS * 32, bat_xs_ctas(CFG))
 spmv_batched_csr_xs(const mgb_csr_batch_item* __restrict__ items, int64_t nitems, int32_t* ws, int init) {
+  constexpr bool I32 = WARPS >= 24;  // 32-bit chunk routine (register budget of 768 threads)
   constexpr int SEG = BAT_SEG[CFG];
   constexpr int64_t CPW = BAT_XS_CPW[CFG];
   constexpr int64_t XCAP = BAT_XS_BYTES / sizeof(T);  // entries per x buffer
@@ -181,13 +191,30 @@ spmv_batched_csr_xs(const mgb_csr_batch_item* __restrict__ items, int64_t nitems
     const int64_t nch = it.nnz / chunk + 1;
     const T* va = static_cast<const T*>(it.values);
     T* y = static_cast<T*>(it.y);
-    for (int64_t c = w; c < nch; c += WARPS) {
-      if (xin)
-        csr::csr_chunk_x<T, SEG>(c, chunk, it.nrows, it.ncols, it.row_offsets, it.column_indices, va,
-                                 csr::XShared<T>{xs}, y, init, stage[w], lane);
-      else
-        csr::csr_chunk_x<T, SEG>(c, chunk, it.nrows, it.ncols, it.row_offsets, it.column_indices, va,
-                                 csr::XGlobal<T>{xg}, y, init, stage[w], lane);
+    const bool too_big = it.nnz >= ((int64_t)1 << 31) - 4096 || it.nrows >= ((int64_t)1 << 31) - 32;
+    if (I32 && too_big) {
+      if (threadIdx.x == 0) ws[3] = 3;
+    } else {
+      for (int64_t c = w; c < nch; c += WARPS) {
+        if constexpr (I32) {
+          const csr::RowRange rows = csr::chunk_rows(c, chunk, it.nrows, it.row_offsets, lane);
+          if (xin)
+            csr::csr_rows_x<T, SEG, csr::XShared<T>, false, int32_t>(rows, it.nrows, it.ncols, it.row_offsets,
+                                                                     it.column_indices, va, csr::XShared<T>{xs}, y,
+                                                                     init, stage[w], lane);
+          else
+            csr::csr_rows_x<T, SEG, csr::XGlobal<T>, false, int32_t>(rows, it.nrows, it.ncols, it.row_offsets,
+                                                                     it.column_indices, va, csr::XGlobal<T>{xg}, y,
+                                                                     init, stage[w], lane);
+        } else {
+          if (xin)
+            csr::csr_chunk_x<T, SEG>(c, chunk, it.nrows, it.ncols, it.row_offsets, it.column_indices, va,
+                                     csr::XShared<T>{xs}, y, init, stage[w], lane);
+          else
+            csr::csr_chunk_x<T, SEG>(c, chunk, it.nrows, it.ncols, it.row_offsets, it.column_indices, va,
+                                     csr::XGlobal<T>{xg}, y, init, stage[w], lane);
+        }
+      }
     }
     __syncthreads();  // buffer `cur` and s_q[cur] are reused by the next fetch
     if constexpr (NBUF == 2) {
@@ -298,13 +325,11 @@ int plan(const mgb_csr_batch_item* items, int64_t nitems, int config, void* work
 
 template <typename T, int CFG>
 int launch_cfg(const mgb_csr_batch_item* items, int64_t nitems, int32_t* ws, int init, cudaStream_t s) {
-  if constexpr (CFG >= BAT_FIRST_XL1) {
+  if constexpr (bat_is_xl1(CFG)) {
     spmv_batched_csr_xl1<T, CFG><<<num_sms() * 3, BAT_WARPS * 32, 0, s>>>(items, nitems, ws, init);
   } else if constexpr (CFG >= BAT_FIRST_XS) {
-    // config 6: one x buffer, two CTAs of 8 warps per SM; config 7: two
-    // buffers (next matrix's x copied during this one), one CTA of 16 warps
-    constexpr int NBUF = CFG == BAT_FIRST_XS ? 1 : 2;
-    constexpr int WARPS = CFG == BAT_FIRST_XS ? 8 : 16;
+    constexpr int NBUF = bat_xs_nbuf(CFG);
+    constexpr int WARPS = bat_xs_warps(CFG);
     constexpr size_t smem = NBUF * BAT_XS_BYTES + WARPS * sizeof(csr::WarpStage<T, BAT_SEG[CFG]>);
     // set once per device (a function attribute, not a stream operation)
     static std::atomic<bool> attr_set[64];
@@ -316,7 +341,7 @@ int launch_cfg(const mgb_csr_batch_item* items, int64_t nitems, int32_t* ws, int
       if (dev >= 0 && dev < 64) attr_set[dev].store(true, std::memory_order_release);
     }
     spmv_batched_csr_xs<T, CFG, NBUF, WARPS>
-        <<<num_sms() * (16 / WARPS), WARPS * 32, smem, s>>>(items, nitems, ws, init);
+        <<<num_sms() * bat_xs_ctas(CFG), WARPS * 32, smem, s>>>(items, nitems, ws, init);
   } else {
     spmv_batched_csr<T, CFG><<<num_sms() * 3, BAT_WARPS * 32, 0, s>>>(items, nitems, ws, init);
   }
@@ -342,7 +367,8 @@ int launch(const mgb_csr_batch_item* items, int64_t nitems, int config, void* wo
     case 6: return launch_cfg<T, 6>(items, nitems, ws, init, s);
     case 7: return launch_cfg<T, 7>(items, nitems, ws, init, s);
     case 8: return launch_cfg<T, 8>(items, nitems, ws, init, s);
-    default: return launch_cfg<T, 9>(items, nitems, ws, init, s);
+    case 9: return launch_cfg<T, 9>(items, nitems, ws, init, s);
+    default: return launch_cfg<T, 10>(items, nitems, ws, init, s);
   }
 }
 

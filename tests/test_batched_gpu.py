@@ -33,7 +33,7 @@ def check(mats, xs, ys, y0s, init, tol):
         assert rel_err(y.cpu().numpy(), ref) <= tol
 
 
-@pytest.mark.parametrize("config", range(10))
+@pytest.mark.parametrize("config", range(11))
 def test_every_config(cuda, config):
     mats, dev, xs, ys, _ = make_batch(60, seed=config)
     y0s = [y.cpu().numpy() for y in ys]
@@ -68,7 +68,7 @@ def test_autotune_and_graph_replay(cuda):
     check(mats, xs, ys, y0s, True, 1e-12)
 
 
-@pytest.mark.parametrize("config", [6, 7])
+@pytest.mark.parametrize("config", [6, 7, 10])
 def test_shared_x_configs_f32_and_wide_x(cuda, config):
     """Matrix-per-CTA configurations keep x in shared memory up to 64 KB;
     wider x (here 20,000 and 40,000 columns) is read from global memory."""
@@ -93,7 +93,7 @@ def test_shared_x_configs_f32_and_wide_x(cuda, config):
         assert err <= 1e-5
 
 
-@pytest.mark.parametrize("config", [6, 7])
+@pytest.mark.parametrize("config", [6, 7, 10])
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
 def test_shared_x_configs_unaligned_x(cuda, config, dtype):
     """x vectors that start one element past a 16-byte boundary are copied
