@@ -257,7 +257,7 @@ def measure_unit_peaks(dev) -> dict:
     """FP64 FMA throughput and random 8-byte gather rate (one 32-byte L1TEX
     sector each) of this GPU, from the library's peak kernels
     (mgb_peak_dfma_f64, mgb_peak_gather_f64) timed with CUDA events; best of
-    5 launches after a warm-up."""
+    3 launches after a warm-up."""
     import ctypes as C
 
     import torch
@@ -269,7 +269,7 @@ def measure_unit_peaks(dev) -> dict:
     stream = torch.cuda.current_stream(dev)
     sh = C.c_void_p(stream.cuda_stream)
 
-    def best_ms(launch, reps=5):
+    def best_ms(launch, reps=3):
         launch()
         torch.cuda.synchronize(dev)
         out = []
@@ -284,7 +284,7 @@ def measure_unit_peaks(dev) -> dict:
 
     blocks = sms * 8
     sink = torch.empty(blocks * tpb, dtype=torch.float64, device=dev)
-    iters = 2048
+    iters = 512  # ~2.4 ms per launch
     ms = best_ms(lambda: _lib.call("mgb_peak_dfma_f64", blocks, iters, C.c_void_p(sink.data_ptr()), sh))
     fma_per_s = blocks * tpb * iters * 8 / (ms * 1e-3)
     table_len = 1 << 21  # 16 MB of doubles: L2-resident, like x of the power-law matrix
@@ -300,7 +300,7 @@ def measure_unit_peaks(dev) -> dict:
             "random_sectors_per_s": gathers_per_s, "sms": sms,
             "how": "mgb_peak_dfma_f64: 8 independent FMA chains per lane, 8 CTAs x 256 threads per SM; "
                    "mgb_peak_gather_f64: 8 random 8-byte loads in flight per lane from a 16 MB table; "
-                   "best of 5 launches, CUDA events"}
+                   "best of 3 launches, CUDA events"}
 
 
 def roofline(hm: dict, vbytes: int, us: float, unit_peaks: dict, x_access: str, traffic=None,

@@ -73,13 +73,18 @@ __global__ void row_stats_kernel(LEN lens, int64_t nrows, int64_t hyb_w,
 // per-entry diagonal bin (c - r + nrows - 1)
 __global__ void csr_diag_kernel(const int32_t* __restrict__ ro, const int32_t* __restrict__ ci, int64_t nrows,
                                 int64_t ncols, int32_t* counts) {
+  MGB_CTA_HIST(h);
+  prim::hist_init(h);
+  __syncthreads();
   for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += (int64_t)gridDim.x * blockDim.x) {
     for (int32_t j = ro[r]; j < ro[r + 1]; j++) {
       const int64_t c = ci[j];
       if (c < 0 || c >= ncols) continue;
-      atomicAdd(counts + (c - r + nrows - 1), 1);
+      prim::hist_add(h, counts, (unsigned long long)(c - r + nrows - 1));
     }
   }
+  __syncthreads();
+  prim::hist_flush(h, counts);
 }
 
 // Diagonal summary: occupied diagonals, true diagonals and their entries,
@@ -120,27 +125,37 @@ __global__ void diag_summary_kernel(const int32_t* __restrict__ counts, int64_t 
 
 __global__ void coo_form_coo(const int32_t* __restrict__ ri, const int32_t* __restrict__ ci, int64_t nnz,
                              int64_t nrows, int64_t ncols, int32_t* lens, int32_t* diag) {
+  MGB_CTA_HIST(h);
+  prim::hist_init(h);
+  __syncthreads();
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += (int64_t)gridDim.x * blockDim.x) {
     const int64_t r = ri[k], c = ci[k];
     if (r < 0 || r >= nrows || c < 0 || c >= ncols) continue;
-    atomicAdd(lens + r, 1);
-    atomicAdd(diag + (c - r + nrows - 1), 1);
+    prim::warp_merged_add(lens, r);
+    prim::hist_add(h, diag, (unsigned long long)(c - r + nrows - 1));
   }
+  __syncthreads();
+  prim::hist_flush(h, diag);
 }
 
 // CSR entries added to existing lengths (the CSR part of HDC)
 __global__ void coo_form_csr(const int32_t* __restrict__ ro, const int32_t* __restrict__ ci, int64_t nrows,
                              int64_t ncols, int32_t* lens, int32_t* diag) {
+  MGB_CTA_HIST(h);
+  prim::hist_init(h);
+  __syncthreads();
   for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += (int64_t)gridDim.x * blockDim.x) {
     int32_t n = 0;
     for (int32_t j = ro[r]; j < ro[r + 1]; j++) {
       const int64_t c = ci[j];
       if (c < 0 || c >= ncols) continue;
       n++;
-      atomicAdd(diag + (c - r + nrows - 1), 1);
+      prim::hist_add(h, diag, (unsigned long long)(c - r + nrows - 1));
     }
     lens[r] += n;
   }
+  __syncthreads();
+  prim::hist_flush(h, diag);
 }
 
 // DIA: thread per row over the diagonals; per-diagonal counts are summed per
@@ -183,16 +198,21 @@ __global__ void coo_form_dia(const int32_t* __restrict__ off, int64_t nd, int64_
 // conversion to COO keeps them)
 __global__ void coo_form_ell(const int32_t* __restrict__ ci, int64_t width, int64_t pitch, int64_t nrows,
                              int64_t ncols, int32_t* lens, int32_t* diag) {
+  MGB_CTA_HIST(h);
+  prim::hist_init(h);
+  __syncthreads();
   for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += (int64_t)gridDim.x * blockDim.x) {
     int32_t n = 0;
     for (int64_t k = 0; k < width; k++) {
       const int64_t c = __ldg(ci + r + pitch * k);
       if (c == MGB_INVALID_INDEX || c < 0 || c >= ncols) continue;
       n++;
-      atomicAdd(diag + (c - r + nrows - 1), 1);
+      prim::hist_add(h, diag, (unsigned long long)(c - r + nrows - 1));
     }
     lens[r] += n;
   }
+  __syncthreads();
+  prim::hist_flush(h, diag);
 }
 
 __global__ void init_stats(unsigned long long* u, double* d, int* i) {

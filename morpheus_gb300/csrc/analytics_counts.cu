@@ -47,29 +47,41 @@ __global__ void csr_row_counts(const int32_t* __restrict__ ro, int64_t nrows, in
 __global__ void coo_row_counts(const int32_t* __restrict__ ri, int64_t nnz, int64_t nrows, int32_t* out) {
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += (int64_t)gridDim.x * blockDim.x) {
     const int32_t r = ri[k];
-    if (r >= 0 && r < nrows) atomicAdd(out + r, 1);
+    if (r >= 0 && r < nrows) prim::warp_merged_add(out, r);
   }
 }
 
 __global__ void csr_diag_counts(const int32_t* __restrict__ ro, const int32_t* __restrict__ ci, int64_t nrows,
                                 int64_t ncols, int32_t* out) {
-  // one warp per row: coalesced column reads for long rows
+  // one warp per row: coalesced column reads for long rows; few hot
+  // diagonals per CTA are counted in shared memory first
+  MGB_CTA_HIST(h);
+  prim::hist_init(h);
+  __syncthreads();
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
   for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < nrows; r += warps) {
     for (int32_t j = ro[r] + lane; j < ro[r + 1]; j += 32) {
       const int64_t c = ci[j];
-      if (c >= 0 && c < ncols) atomicAdd(out + (c - r + nrows - 1), 1);
+      if (c >= 0 && c < ncols) prim::hist_add(h, out, (unsigned long long)(c - r + nrows - 1));
     }
   }
+  __syncthreads();
+  prim::hist_flush(h, out);
 }
 
 __global__ void coo_diag_counts(const int32_t* __restrict__ ri, const int32_t* __restrict__ ci, int64_t nnz,
                                 int64_t nrows, int64_t ncols, int32_t* out) {
+  MGB_CTA_HIST(h);
+  prim::hist_init(h);
+  __syncthreads();
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += (int64_t)gridDim.x * blockDim.x) {
     const int64_t r = ri[k], c = ci[k];
-    if (r >= 0 && r < nrows && c >= 0 && c < ncols) atomicAdd(out + (c - r + nrows - 1), 1);
+    if (r >= 0 && r < nrows && c >= 0 && c < ncols)
+      prim::hist_add(h, out, (unsigned long long)(c - r + nrows - 1));
   }
+  __syncthreads();
+  prim::hist_flush(h, out);
 }
 
 __global__ void count_above(const int32_t* __restrict__ v, int64_t n, int32_t thr, unsigned long long* cnt) {
@@ -147,6 +159,9 @@ __global__ void ell_row_counts(const int32_t* __restrict__ ci, int64_t width, in
 template <typename T>
 __global__ void ell_diag_counts(const int32_t* __restrict__ ci, const T* __restrict__ v, int64_t width,
                                 int64_t pitch, int64_t nrows, int64_t ncols, int32_t* __restrict__ out) {
+  MGB_CTA_HIST(h);
+  prim::hist_init(h);
+  __syncthreads();
   for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += (int64_t)gridDim.x * blockDim.x) {
     int64_t k = 0;
     for (int64_t n = 0; n < width; n++) {
@@ -156,9 +171,11 @@ __global__ void ell_diag_counts(const int32_t* __restrict__ ci, const T* __restr
     for (int64_t n = 0; n < k; n++) {
       const int64_t c = __ldg(ci + r + pitch * n);
       if (c != MGB_INVALID_INDEX && __ldg(v + r + pitch * n) != T(0) && c >= 0 && c < ncols)
-        atomicAdd(out + (c - r + nrows - 1), 1);
+        prim::hist_add(h, out, (unsigned long long)(c - r + nrows - 1));
     }
   }
+  __syncthreads();
+  prim::hist_flush(h, out);
 }
 
 // ---- per-format launchers (descriptor checks, then the kernels) ----------

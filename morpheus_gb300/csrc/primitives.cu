@@ -115,11 +115,18 @@ __global__ void sum_i32_kernel(const int32_t* __restrict__ in, int64_t n, unsign
   if ((threadIdx.x & 31) == 0) atomicAdd(out, (unsigned long long)sacc);
 }
 
+// counts[k] += 1 for every key in [0, nbins); few hot keys per CTA are
+// counted in shared memory first (CtaHist)
 __global__ void histogram_kernel(const int32_t* __restrict__ keys, int64_t n, int32_t* counts, int64_t nbins) {
+  MGB_CTA_HIST(h);
+  hist_init(h);
+  __syncthreads();
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const int32_t k = keys[i];
-    if (k >= 0 && k < nbins) atomicAdd(counts + k, 1);
+    if (k >= 0 && k < nbins) hist_add(h, counts, (unsigned long long)k);
   }
+  __syncthreads();
+  hist_flush(h, counts);
 }
 
 __global__ void sorted_flags_kernel(const int32_t* __restrict__ r, const int32_t* __restrict__ c, int64_t n,

@@ -77,6 +77,77 @@ int to_host(const T* d, T* h, cudaStream_t s) {
   return MGB_SUCCESS;
 }
 
+// ---- counting into few hot bins --------------------------------------------
+// A histogram whose entries fall into few distinct bins per CTA (the
+// diagonals of a banded or stencil matrix: 27 bins for a 27-point stencil,
+// however many entries) serialises on global atomics.  CtaHist counts in
+// shared memory first: lanes of a warp holding the same key are merged
+// (__match_any_sync), the warp's leader for that key adds into an
+// open-addressing table of HIST_SLOTS (key, count) pairs, and the CTA
+// flushes the table with one global atomic per occupied slot.  A key that
+// finds no free slot within HIST_PROBES probes marks the table full and,
+// like every key after it, goes straight to the global counter, so the
+// counts are exact in every case and scattered keys pay little for the try.
+constexpr int HIST_SLOTS = 2048;
+constexpr int HIST_PROBES = 8;
+constexpr unsigned long long HIST_EMPTY = ~0ull;
+
+struct CtaHist {
+  unsigned long long* keys;  // HIST_SLOTS keys, HIST_EMPTY where free
+  int32_t* counts;           // HIST_SLOTS counts
+  int* full;                 // set once a key found no slot
+};
+
+// every thread of the CTA, followed by __syncthreads()
+__device__ __forceinline__ void hist_init(CtaHist h) {
+  for (int i = threadIdx.x; i < HIST_SLOTS; i += blockDim.x) {
+    h.keys[i] = HIST_EMPTY;
+    h.counts[i] = 0;
+  }
+  if (threadIdx.x == 0) *h.full = 0;
+}
+
+// counts one occurrence of key (global[key] += 1, in the end)
+__device__ __forceinline__ void hist_add(CtaHist h, int32_t* global, unsigned long long key) {
+  const unsigned same = __match_any_sync(__activemask(), key);
+  if ((int)(threadIdx.x & 31) != __ffs(same) - 1) return;  // one lane per distinct key adds
+  const int inc = __popc(same);
+  if (!*reinterpret_cast<volatile int*>(h.full)) {
+    unsigned slot = (unsigned)((key * 0x9E3779B97F4A7C15ull) >> 53) & (HIST_SLOTS - 1);
+    for (int p = 0; p < HIST_PROBES; p++) {
+      const unsigned long long prev = atomicCAS(h.keys + slot, HIST_EMPTY, key);
+      if (prev == HIST_EMPTY || prev == key) {
+        atomicAdd(h.counts + slot, inc);
+        return;
+      }
+      slot = (slot + 1) & (HIST_SLOTS - 1);
+    }
+    *reinterpret_cast<volatile int*>(h.full) = 1;
+  }
+  atomicAdd(global + key, inc);
+}
+
+// every thread of the CTA, after a __syncthreads() that follows the last hist_add
+__device__ __forceinline__ void hist_flush(CtaHist h, int32_t* global) {
+  for (int i = threadIdx.x; i < HIST_SLOTS; i += blockDim.x) {
+    const unsigned long long k = h.keys[i];
+    if (k != HIST_EMPTY && h.counts[i]) atomicAdd(global + k, h.counts[i]);
+  }
+}
+
+// global[key] += 1 with the lanes of a warp holding the same key merged
+// (row counts of row-sorted entries: consecutive lanes share a row)
+__device__ __forceinline__ void warp_merged_add(int32_t* global, int64_t key) {
+  const unsigned same = __match_any_sync(__activemask(), (unsigned long long)key);
+  if ((int)(threadIdx.x & 31) == __ffs(same) - 1) atomicAdd(global + key, __popc(same));
+}
+
+#define MGB_CTA_HIST(name)                                  \
+  __shared__ unsigned long long name##_keys[::mgb::prim::HIST_SLOTS]; \
+  __shared__ int32_t name##_counts[::mgb::prim::HIST_SLOTS];          \
+  __shared__ int name##_full;                                         \
+  const ::mgb::prim::CtaHist name{name##_keys, name##_counts, &name##_full}
+
 inline unsigned blocks_for(int64_t n, int threads, int64_t cap = 1 << 20) {
   int64_t b = (n + threads - 1) / threads;
   if (b < 1) b = 1;
