@@ -37,55 +37,86 @@ __device__ __forceinline__ T block_sum(T v) {
   return v;  // valid in thread 0
 }
 
+// 16-byte streaming load / store of V = 16 / sizeof(T) elements at vector index i
+template <typename T>
+__device__ __forceinline__ void ld16(const T* p, int64_t i, T* a) {
+  if constexpr (sizeof(T) == 8) {
+    const double2 v = __ldcs(reinterpret_cast<const double2*>(p) + i);
+    a[0] = v.x; a[1] = v.y;
+  } else {
+    const float4 v = __ldcs(reinterpret_cast<const float4*>(p) + i);
+    a[0] = v.x; a[1] = v.y; a[2] = v.z; a[3] = v.w;
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void st16(T* p, int64_t i, const T* a) {
+  if constexpr (sizeof(T) == 8) __stcs(reinterpret_cast<double2*>(p) + i, make_double2(a[0], a[1]));
+  else __stcs(reinterpret_cast<float4*>(p) + i, make_float4(a[0], a[1], a[2], a[3]));
+}
+
 // MODE 0: dot(x, y); MODE 1: dot(x, x); MODE 2: sum(x)
+// Each grid-stride step of the vector body issues eight 16-byte loads per
+// thread before it accumulates (U vectors of x, and of y for MODE 0), so an
+// SM with 1,024 threads keeps 128 KB of loads in flight.  Four accumulators
+// per thread.  Measured on x.y over 2^26 doubles: 7.0 TB/s of reads with
+// U = 4 at 4 CTAs per SM, against 6.4-6.9 TB/s with 1-2 and 5.6-6.2 TB/s
+// at 2 or 8 CTAs per SM.
 template <typename T, int MODE>
-__global__ void __launch_bounds__(RED_THREADS)
+__global__ void __launch_bounds__(RED_THREADS, 4)
 reduce_partial(int64_t n, const T* __restrict__ x, const T* __restrict__ y,
                T* __restrict__ partial) {
-  T acc0 = T(0), acc1 = T(0);
+  T acc[4] = {T(0), T(0), T(0), T(0)};
   const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t nth = (int64_t)gridDim.x * blockDim.x;
   // 16-byte vector body when both pointers are 16-byte aligned
   constexpr int V = 16 / sizeof(T);
+  constexpr int U = (MODE == 0) ? 4 : 8;
   const bool vec = (reinterpret_cast<uintptr_t>(x) % 16 == 0) &&
                    (MODE != 0 || reinterpret_cast<uintptr_t>(y) % 16 == 0);
   int64_t done = 0;
   if (vec) {
     const int64_t nv = n / V;
-    for (int64_t i = tid; i < nv; i += nth) {
-      T a[V], b[V];
-      if constexpr (sizeof(T) == 8) {
-        const double2 va = __ldcs(reinterpret_cast<const double2*>(x) + i);
-        a[0] = va.x; a[1] = va.y;
-        if constexpr (MODE == 0) {
-          const double2 vb = __ldcs(reinterpret_cast<const double2*>(y) + i);
-          b[0] = vb.x; b[1] = vb.y;
-        }
-      } else {
-        const float4 va = __ldcs(reinterpret_cast<const float4*>(x) + i);
-        a[0] = va.x; a[1] = va.y; a[2] = va.z; a[3] = va.w;
-        if constexpr (MODE == 0) {
-          const float4 vb = __ldcs(reinterpret_cast<const float4*>(y) + i);
-          b[0] = vb.x; b[1] = vb.y; b[2] = vb.z; b[3] = vb.w;
-        }
+    int64_t i = tid;
+#pragma unroll 1
+    for (; i + (U - 1) * nth < nv; i += U * nth) {
+      T a[U][V], b[U][V];
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        ld16(x, i + u * nth, a[u]);
+        if constexpr (MODE == 0) ld16(y, i + u * nth, b[u]);
       }
 #pragma unroll
+      for (int u = 0; u < U; u++)
+#pragma unroll
+        for (int k = 0; k < V; k++) {
+          T& s = acc[(u * V + k) & 3];
+          if constexpr (MODE == 0) s = fmadd(a[u][k], b[u][k], s);
+          else if constexpr (MODE == 1) s = fmadd(a[u][k], a[u][k], s);
+          else s += a[u][k];
+        }
+    }
+    for (; i < nv; i += nth) {
+      T a[V], b[V];
+      ld16(x, i, a);
+      if constexpr (MODE == 0) ld16(y, i, b);
+#pragma unroll
       for (int k = 0; k < V; k++) {
-        T& acc = (k & 1) ? acc1 : acc0;
-        if (MODE == 0) acc = fmadd(a[k], b[k], acc);
-        else if (MODE == 1) acc = fmadd(a[k], a[k], acc);
-        else acc += a[k];
+        T& s = acc[k & 3];
+        if constexpr (MODE == 0) s = fmadd(a[k], b[k], s);
+        else if constexpr (MODE == 1) s = fmadd(a[k], a[k], s);
+        else s += a[k];
       }
     }
     done = nv * V;
   }
   for (int64_t i = done + tid; i < n; i += nth) {
     const T a = __ldcs(x + i);
-    if (MODE == 0) acc0 = fmadd(a, __ldcs(y + i), acc0);
-    else if (MODE == 1) acc0 = fmadd(a, a, acc0);
-    else acc0 += a;
+    if (MODE == 0) acc[0] = fmadd(a, __ldcs(y + i), acc[0]);
+    else if (MODE == 1) acc[0] = fmadd(a, a, acc[0]);
+    else acc[0] += a;
   }
-  const T s = block_sum(acc0 + acc1);
+  const T s = block_sum((acc[0] + acc[1]) + (acc[2] + acc[3]));
   if (threadIdx.x == 0) partial[blockIdx.x] = s;
 }
 
@@ -146,17 +177,37 @@ int dot_any(int64_t n, const T* x, const T* y, T* out, cudaStream_t s, bool host
 
 // MODE 0: alpha*x + beta*y, 1: x + beta*y, 2: alpha*x + y
 template <typename T, int MODE>
-__global__ void waxpby_kernel(int64_t n, T alpha, const T* __restrict__ x, T beta,
-                              const T* __restrict__ y, T* __restrict__ w) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const T a = __ldcs(x + i), b = __ldcs(y + i);
-    T r;
-    if (MODE == 1) r = fmadd(beta, b, a);
-    else if (MODE == 2) r = fmadd(alpha, a, b);
-    else r = fmadd(alpha, a, beta * b);
-    __stcs(w + i, r);
+__device__ __forceinline__ T wax(T alpha, T a, T beta, T b) {
+  if constexpr (MODE == 1) return fmadd(beta, b, a);
+  else if constexpr (MODE == 2) return fmadd(alpha, a, b);
+  else return fmadd(alpha, a, beta * b);
+}
+
+// w may be x or y (in-place updates): each element is read and written by
+// the same thread at the same index, so the pointers carry no __restrict__.
+// 16-byte loads and stores when all three are 16-byte aligned.
+template <typename T, int MODE>
+__global__ void waxpby_kernel(int64_t n, T alpha, const T* x, T beta, const T* y, T* w) {
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+  constexpr int V = 16 / sizeof(T);
+  const bool vec = ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(y) |
+                     reinterpret_cast<uintptr_t>(w)) % 16) == 0;
+  int64_t done = 0;
+  if (vec) {
+    const int64_t nv = n / V;
+    for (int64_t i = tid; i < nv; i += nth) {
+      T a[V], b[V], r[V];
+      ld16(x, i, a);
+      ld16(y, i, b);
+#pragma unroll
+      for (int k = 0; k < V; k++) r[k] = wax<T, MODE>(alpha, a[k], beta, b[k]);
+      st16(w, i, r);
+    }
+    done = nv * V;
   }
+  for (int64_t i = done + tid; i < n; i += nth)
+    __stcs(w + i, wax<T, MODE>(alpha, __ldcs(x + i), beta, __ldcs(y + i)));
 }
 
 template <typename T>
@@ -165,7 +216,7 @@ int launch_waxpby(int64_t n, T alpha, const T* x, T beta, const T* y, T* w, cuda
   if (n == 0) return MGB_SUCCESS;
   MGB_REQUIRE(x && y && w, MGB_ERR_BAD_ARGUMENT);
   int64_t blocks = (n + 255) / 256;
-  const int64_t cap = (int64_t)num_sms() * 16;
+  const int64_t cap = (int64_t)num_sms() * 8;  // one resident wave of 2,048 threads per SM
   if (blocks > cap) blocks = cap;
   if (alpha == T(1))
     waxpby_kernel<T, 1><<<(unsigned)blocks, 256, 0, s>>>(n, alpha, x, beta, y, w);
