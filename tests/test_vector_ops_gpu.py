@@ -67,3 +67,41 @@ def test_waxpby(cuda, alpha, beta, dtype):
         mgb.waxpby(n, alpha, torch.from_numpy(x).cuda(), beta, torch.from_numpy(y).cuda(), w)
         tol = 1e-13 if dtype == np.float64 else 1e-5
         assert np.max(np.abs(w.cpu().numpy().astype(np.float64) - w_ref)) <= tol * 10
+
+
+# FP64 reduce splits each large vector between FP64 adds and an exact
+# fixed-point accumulation on the integer pipe; the split engages once every
+# thread of the grid sees at least one 16-element step (a few million elements).
+N_SPLIT = (1 << 22) + 3
+
+
+def test_reduce_wide_exponent_range(cuda):
+    import math
+    rng = np.random.default_rng(11)
+    x = rng.standard_normal(N_SPLIT) * np.exp2(rng.integers(-600, 600, N_SPLIT))
+    got = mgb.reduce(torch.from_numpy(x).cuda(), N_SPLIT)
+    exact = math.fsum(x)  # correctly rounded
+    assert abs(got - exact) <= 1e-14 * float(np.sum(np.abs(x)))
+    # exact cancellation: the result stays within the same bound of zero
+    y = np.concatenate([x, -x])
+    assert abs(mgb.reduce(torch.from_numpy(y).cuda(), y.size)) <= 1e-14 * float(np.sum(np.abs(y)))
+
+
+@pytest.mark.parametrize("special", ["inf", "-inf", "nan", "inf-inf"])
+def test_reduce_special_values_propagate(cuda, special):
+    """Inf and NaN reach the result from either share of the split (the
+    positions below fall in both, as in the Serial sum)."""
+    rng = np.random.default_rng(12)
+    base = torch.from_numpy(rng.uniform(-1, 1, N_SPLIT)).cuda()
+    for pos in rng.integers(0, N_SPLIT, 24):
+        x = base.clone()
+        if special == "inf-inf":
+            x[int(pos)] = np.inf
+            x[(int(pos) + 7) % N_SPLIT] = -np.inf
+        else:
+            x[int(pos)] = float(special)
+        got = mgb.reduce(x, N_SPLIT)
+        if special in ("nan", "inf-inf"):
+            assert np.isnan(got), (special, int(pos))
+        else:
+            assert got == float(special), (special, int(pos), got)
