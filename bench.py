@@ -552,6 +552,16 @@ def run_suite(args, rank: int, world: int, local_rank: int):
     switch_ms = (time.perf_counter() - t0) * 1e3
     if status != mgb.conversion_error_e.CONV_SUCCESS:
         raise SystemExit(f"selector switch failed: {status}")
+    # the same switch again on a second DynamicMatrix over the CSR container
+    # (the first call also pays one-time costs: allocator pool growth, the
+    # selector's weights)
+    dyn2 = mgb.DynamicMatrix(A_csr)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    mgb.convert(dyn2, AUTO_FORMAT)
+    torch.cuda.synchronize()
+    switch_warm_ms = (time.perf_counter() - t0) * 1e3
+    del dyn2
     sel_fmt = FORMAT_NAMES[dyn.active_index()]
     M_sel = dyn.active()
     hm_sel = mgb.matrix_to_host(M_sel)
@@ -625,7 +635,7 @@ def run_suite(args, rank: int, world: int, local_rank: int):
                         "roofline": roofline(S, 8, csr_ms * 1e3, unit_peaks, "banded",
                                              profile_traffic("c3_stencil27_160_csr_f64"))},
         "speedup_vs_csr_default": csr_ms / kernel_ms,
-        "selector_switch_ms": switch_ms,
+        "selector_switch_ms": switch_warm_ms, "selector_switch_first_call_ms": switch_ms,
         "roofline": roofline(hm_sel, 8, us, unit_peaks, "banded",
                              profile_traffic(f"c3_stencil27_160_{sel_fmt}_f64")),
         "unit_peaks": unit_peaks,
@@ -710,6 +720,8 @@ def run_suite(args, rank: int, world: int, local_rank: int):
             per.append(selector_entry(args.selector_test))
         # conversions at the benchmark sizes against the Serial convert
         per.append(convert_entry(dev, ck))
+        # dot / reduce / waxpby on 512 MB vectors
+        per.extend(vector_entry(dev, stream, unit_peaks, ck))
     line["per_config"] = per
     line["suite_seconds"] = time.time() - t_start
     print(json.dumps(line), flush=True)
@@ -723,6 +735,111 @@ def headline_config(S: dict, fmt: str, world: int) -> dict:
             "format": fmt.upper(), "format_choice": "learned selector (convert(dyn, AUTO_FORMAT))",
             "nrows": S["nrows"], "ncols": S["ncols"], "nnz": int(S["nnz"]),
             "l2": "inputs larger than L2 (no flush needed)", "parallelism": f"replicas x{world}"}
+
+
+def vector_entry(dev, stream, unit_peaks, cpu_budget: float, n: int = 1 << 26) -> list:
+    """dot / reduce / waxpby on 2^26-element FP64 vectors (512 MB each, larger
+    than L2), device-resident, timed with CUDA events over 20 launches after a
+    warm-up.  Each names its binding unit: HBM (algorithmic bytes / copy
+    peak) or the FP64 pipe (FP64 operations / measured FMA rate; an FP64 add
+    costs the same as an FMA).  The reduce splits its elements between FP64
+    adds and exact integer-pipe accumulation, so its FP64 floor is that of the
+    FP64 share (9 of 16).  CPU: the oracle's Serial restatement, one core."""
+    import ctypes as C
+
+    import torch
+
+    import morpheus_gb300 as mgb
+    from morpheus_gb300 import _lib
+    from oracle import oracle as O
+    lib = _lib.load()
+    rng = np.random.default_rng(21)
+    x_np, y_np = rng.uniform(-1, 1, n), rng.uniform(-1, 1, n)
+    x, y = torch.from_numpy(x_np).to(dev), torch.from_numpy(y_np).to(dev)
+    w = torch.empty_like(x)
+    out = torch.zeros(1, dtype=torch.float64, device=dev)
+    sh = C.c_void_p(stream.cuda_stream)
+    X, Y, W, R = (C.c_void_p(t.data_ptr()) for t in (x, y, w, out))
+
+    def timed_us(launch, k=20):
+        for _ in range(3):
+            launch()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(k):
+            launch()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        return e0.elapsed_time(e1) / k * 1e3
+
+    def cpu_us(fn):
+        t0 = time.perf_counter()
+        reps = 0
+        while reps < 1 or (time.perf_counter() - t0 < min(cpu_budget, 2.0) and reps < 5):
+            fn()
+            reps += 1
+        return (time.perf_counter() - t0) / reps * 1e6
+
+    def check(name, code):
+        if code != 0:
+            raise SystemExit(f"{name} failed with status {code}")
+
+    ops = [
+        ("dot_xy", lambda: check("dot", lib.mgb_dot_f64_async(n, X, Y, R, sh)), 16 * n, n,
+         lambda: O.dot(n, x_np, y_np), lambda: float(out.item())),
+        ("dot_xx", lambda: check("dot", lib.mgb_dot_f64_async(n, X, X, R, sh)), 8 * n, n,
+         lambda: O.dot(n, x_np, x_np), lambda: float(out.item())),
+        ("reduce", lambda: check("reduce", lib.mgb_reduce_f64_async(X, n, R, sh)), 8 * n, n * 9 // 16,
+         lambda: O.reduce(x_np, n), lambda: float(out.item())),
+        ("waxpby_alpha_beta", lambda: check("waxpby", lib.mgb_waxpby_f64(n, 2.15, X, -3.2, Y, W, sh)), 24 * n, 2 * n,
+         None, None),
+        ("waxpby_alpha_1", lambda: check("waxpby", lib.mgb_waxpby_f64(n, 2.15, X, 1.0, Y, W, sh)), 24 * n, n,
+         None, None),
+    ]
+    res = []
+    for name, launch, nbytes, fp64_ops, cpu_fn, gpu_val in ops:
+        us = timed_us(launch)
+        floors = {"hbm": nbytes / (unit_peaks["hbm_gbs"] * 1e9) * 1e6,
+                  "fp64_pipe": fp64_ops / unit_peaks["fp64_fma_per_s"] * 1e6}
+        unit = max(floors, key=floors.get)
+        e = {"config": f"vector_{name}_2^26_f64", "us": us, "GB/s": nbytes / (us * 1e-6) / 1e9,
+             "roofline": {"bound": "hbm", "achieved": nbytes / (us * 1e-6) / 1e9, "peak": unit_peaks["hbm_gbs"],
+                          "unit": "GB/s", "frac": nbytes / (us * 1e-6) / 1e9 / unit_peaks["hbm_gbs"],
+                          "algorithmic_bytes_per_launch": nbytes, "fp64_ops_per_launch": fp64_ops,
+                          "binding_unit": unit, "floor_us": floors[unit], "frac_of_binding_unit": floors[unit] / us,
+                          "floors_us": floors},
+             "l2": "inputs larger than L2"}
+        tr = profile_traffic(f"vector_{name}_2^26_f64")
+        e["roofline"]["traffic"] = None if tr is None else tr[0]
+        if tr is not None:
+            e["roofline"]["traffic_source"] = tr[1]
+        if cpu_fn is not None:
+            import math
+            launch()
+            torch.cuda.synchronize(dev)
+            got = gpu_val()
+            want = cpu_fn()
+            terms = x_np if name == "reduce" else x_np * (y_np if name == "dot_xy" else x_np)
+            exact = math.fsum(terms)  # correctly rounded sum of the (rounded) terms
+            scale = float(np.sum(np.abs(terms)))
+            # errors relative to sum |terms|, against the correctly rounded sum:
+            # the GPU's and the oracle's (the Serial restatement, one long
+            # recursive sum)
+            e["rel_err_vs_fsum"] = abs(got - exact) / scale
+            e["oracle_rel_err_vs_fsum"] = abs(want - exact) / scale
+            if cpu_budget > 0:
+                cu = cpu_us(cpu_fn)
+                e["cpu_baseline"] = {"value": nbytes / (cu * 1e-6) / 1e9, "unit": "GB/s", "cores": 1, "kind": "port",
+                                     "sample": "full vectors, Serial restatement in oracle/oracle.cpp"}
+        else:
+            w_ref = np.empty(n)
+            a, b = (2.15, -3.2) if name == "waxpby_alpha_beta" else (2.15, 1.0)
+            O.waxpby(n, a, x_np, b, y_np, w_ref)
+            e["max_abs_err_vs_oracle"] = float(np.max(np.abs(w.cpu().numpy() - w_ref)))
+        res.append(e)
+    del x, y, w
+    return res
 
 
 def batched_entry(args, dev, stream, unit_peaks, cpu_budget) -> dict:
