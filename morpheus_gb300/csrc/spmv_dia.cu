@@ -30,6 +30,12 @@ constexpr int DIA_OFF_CHUNK = 512;
 // groups of 2 or 4 raise the register count and lower occupancy (87 us
 // plain, 93-97 us grouped).
 template <typename T> constexpr int kDiaUnroll = sizeof(T) == 4 ? 1 : 2;
+// Resident CTAs of 256 threads per SM the kernel is compiled for (0: no
+// register cap).  FP64: 8 (32 registers, a few bytes of spills), the FP64
+// pipe fed by 64 warps: 27-point stencil DIA 197 -> 195 us, HDC 220 -> 209 us
+// (5 / 6 CTAs: 199 / 196 us).  FP32 is fastest uncapped (40 registers:
+// 87 us; capped at 5-8 CTAs: 88.5-95.6 us).
+template <typename T> constexpr int kDiaMinBlocks = sizeof(T) == 4 ? 0 : 8;
 
 template <typename T> struct Vec;
 template <> struct Vec<double> { using type = double2; static constexpr int n = 2; };
@@ -63,7 +69,7 @@ __device__ __forceinline__ void dia_load(const T* vp, int64_t row0, int64_t nrow
 // One thread = RPT consecutive rows (vector path, requires pitch % RPT == 0
 // and an aligned values pointer) or RPT = 1 (scalar path).
 template <typename T, int RPT, bool HDC>
-__global__ void __launch_bounds__(DIA_THREADS)
+__global__ void __launch_bounds__(DIA_THREADS, kDiaMinBlocks<T>)
 spmv_dia_rows(int64_t nrows, int64_t ncols, int ndiags, int64_t pitch,
               const int32_t* __restrict__ offs, const T* __restrict__ vals,
               const int32_t* __restrict__ cro, const int32_t* __restrict__ cci,
