@@ -66,8 +66,10 @@ template <> struct IdxVec<1> {
   static __device__ __forceinline__ void load(const int32_t* p, int32_t* o) { o[0] = __ldcs(p); }
 };
 
-template <typename T, int RPT>
-__global__ void __launch_bounds__(ELL_THREADS)
+// MINB: resident CTAs of 256 threads per SM the kernel is compiled for (0:
+// no register cap); the launcher picks it.
+template <typename T, int RPT, int MINB>
+__global__ void __launch_bounds__(ELL_THREADS, MINB)
 spmv_ell_rows(int64_t nrows, int64_t ncols, int64_t width, int64_t pitch,
               const int32_t* __restrict__ ci, const T* __restrict__ va,
               const T* __restrict__ x, T* __restrict__ y, int init) {
@@ -112,6 +114,22 @@ spmv_ell_rows(int64_t nrows, int64_t ncols, int64_t width, int64_t pitch,
 
 }  // namespace
 
+template <typename T, int MINB>
+int launch_ell_rows(const mgb_ell* A, const T* x, T* y, int init, cudaStream_t s, int64_t blocks, int rpt) {
+  const T* va = static_cast<const T*>(A->values);
+  if (rpt == 4)
+    spmv_ell_rows<T, 4, MINB><<<(unsigned)blocks, ELL_THREADS, 0, s>>>(
+        A->nrows, A->ncols, A->width, A->pitch, A->column_indices, va, x, y, init);
+  else if (rpt == 2)
+    spmv_ell_rows<T, 2, MINB><<<(unsigned)blocks, ELL_THREADS, 0, s>>>(
+        A->nrows, A->ncols, A->width, A->pitch, A->column_indices, va, x, y, init);
+  else
+    spmv_ell_rows<T, 1, MINB><<<(unsigned)blocks, ELL_THREADS, 0, s>>>(
+        A->nrows, A->ncols, A->width, A->pitch, A->column_indices, va, x, y, init);
+  MGB_LAUNCH_CHECK();
+  return MGB_SUCCESS;
+}
+
 template <typename T>
 int launch_ell(const mgb_ell* A, const T* x, T* y, int init, cudaStream_t s) {
   MGB_REQUIRE(A != nullptr, MGB_ERR_BAD_ARGUMENT);
@@ -130,18 +148,18 @@ int launch_ell(const mgb_ell* A, const T* x, T* y, int init, cudaStream_t s) {
   int64_t blocks = (groups + ELL_THREADS - 1) / ELL_THREADS;
   const int64_t cap = (int64_t)num_sms() * 64;
   if (blocks > cap) blocks = cap;
-  const T* va = static_cast<const T*>(A->values);
-  if (vec4)
-    spmv_ell_rows<T, 4><<<(unsigned)blocks, ELL_THREADS, 0, s>>>(
-        A->nrows, A->ncols, A->width, A->pitch, A->column_indices, va, x, y, init);
-  else if (vec2)
-    spmv_ell_rows<T, 2><<<(unsigned)blocks, ELL_THREADS, 0, s>>>(
-        A->nrows, A->ncols, A->width, A->pitch, A->column_indices, va, x, y, init);
-  else
-    spmv_ell_rows<T, 1><<<(unsigned)blocks, ELL_THREADS, 0, s>>>(
-        A->nrows, A->ncols, A->width, A->pitch, A->column_indices, va, x, y, init);
-  MGB_LAUNCH_CHECK();
-  return MGB_SUCCESS;
+  // Register caps (measured, 27-point stencil in ELL / power-law HYB at the
+  // p90 width): FP32 at 8 CTAs per SM, 178 -> 173 us / 252 -> 240 us.  FP64
+  // at 6 CTAs per SM where at least half the slots hold entries (FMA-heavy:
+  // stencil 258 -> 241 us), uncapped for mostly-padding slabs (HYB p90: 277
+  // us uncapped, 297 us at 6 CTAs).
+  if constexpr (sizeof(T) == 4) {
+    return launch_ell_rows<T, 8>(A, x, y, init, s, blocks, rpt);
+  } else {
+    const bool dense = 2 * A->nnz >= A->nrows * A->width;
+    if (dense) return launch_ell_rows<T, 6>(A, x, y, init, s, blocks, rpt);
+    return launch_ell_rows<T, 0>(A, x, y, init, s, blocks, rpt);
+  }
 }
 
 template int launch_ell<double>(const mgb_ell*, const double*, double*, int, cudaStream_t);
