@@ -9,6 +9,11 @@ own gradient and Adam kernels, and evaluates on held-out seeds against
 exhaustive timing (regret), against CSR-only, and against the rule-based
 selector (DIA / HDC / ELL / CSR by three feature thresholds tuned on the
 training set, selector.rule_select).
+
+--select picks epochs, learning rate and initialisation seed from a small
+grid by the mean regret on the last fifth of the training matrices (the
+held-out test matrices play no part), then trains on all of them.
+--corpus-in reuses a corpus saved by --corpus-out instead of timing a new one.
 """
 from __future__ import annotations
 
@@ -22,6 +27,36 @@ import numpy as np
 from . import corpus, selector
 
 
+GRID = {"epochs": (400, 1000, 2000), "lr": (1e-3, 3e-3), "seed": (0, 1, 2)}
+def load_corpus(path: str):
+    """The training and test parts of a corpus saved with --corpus-out."""
+    d = np.load(path)
+
+    def part(X, F, T, D):
+        desc = [{"family": str(f)} for f in d[D]] if D in d.files else [{"family": "?"}] * len(d[X])
+        return {"X": d[X], "feasible": d[F], "times": d[T], "labels": np.argmin(d[T], axis=1), "desc": desc}
+    return part("Xtr", "Ftr", "Ttr", "Dtr"), part("Xte", "Fte", "Tte", "Dte")
+
+
+def select_hyperparameters(tr, mu, sigma) -> dict:
+    """Grid over epochs x learning rate x seed, scored by mean regret on the
+    last fifth of the training matrices after training on the rest."""
+    n = len(tr["labels"])
+    cut = n - n // 5
+    fit = {k: tr[k][:cut] for k in ("X", "labels", "feasible", "times")}
+    val = {k: tr[k][cut:] for k in ("X", "labels", "feasible", "times")}
+    best = None
+    for epochs in GRID["epochs"]:
+        for lr in GRID["lr"]:
+            for seed in GRID["seed"]:
+                sel = selector.Selector.random(mu, sigma, seed=seed)
+                sel.train(fit["X"], fit["labels"], fit["feasible"], epochs=epochs, lr=lr, seed=seed)
+                r = selector.evaluate(val["times"], sel.predict(val["X"], val["feasible"]))["mean_regret"]
+                if best is None or r < best["validation_mean_regret"]:
+                    best = {"epochs": epochs, "lr": lr, "seed": seed, "validation_mean_regret": r}
+    return best
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--train", type=int, default=2000)
@@ -32,20 +67,33 @@ def main(argv=None):
     ap.add_argument("--out", default=selector.DEFAULT_WEIGHTS)
     ap.add_argument("--report", default="selector_report.json")
     ap.add_argument("--corpus-out", default=None)
+    ap.add_argument("--corpus-in", default=None)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--select", action="store_true")
     args = ap.parse_args(argv)
 
     t0 = time.time()
-    tr = corpus.build(args.train, seed0=0, reps=args.reps, log=print)
-    te = corpus.build(args.test, seed0=1_000_000, reps=args.reps, log=print)
+    if args.corpus_in:
+        tr, te = load_corpus(args.corpus_in)
+    else:
+        tr = corpus.build(args.train, seed0=0, reps=args.reps, log=print)
+        te = corpus.build(args.test, seed0=1_000_000, reps=args.reps, log=print)
     t_corpus = time.time() - t0
     if args.corpus_out:
         np.savez_compressed(args.corpus_out, Xtr=tr["X"], Ftr=tr["feasible"], Ttr=tr["times"], Xte=te["X"],
-                 Fte=te["feasible"], Tte=te["times"])
+                            Fte=te["feasible"], Tte=te["times"],
+                            Dtr=np.array([d["family"] for d in tr["desc"]]),
+                            Dte=np.array([d["family"] for d in te["desc"]]))
 
     mu, sigma = tr["X"].mean(0), tr["X"].std(0) + 1e-3
-    sel = selector.Selector.random(mu, sigma, seed=0)
+    selection = None
+    if args.select:
+        selection = select_hyperparameters(tr, mu, sigma)
+        args.epochs, args.lr, args.seed = selection["epochs"], selection["lr"], selection["seed"]
+        print("selected", json.dumps(selection), flush=True)
+    sel = selector.Selector.random(mu, sigma, seed=args.seed)
     t1 = time.time()
-    hist = sel.train(tr["X"], tr["labels"], tr["feasible"], epochs=args.epochs, lr=args.lr)
+    hist = sel.train(tr["X"], tr["labels"], tr["feasible"], epochs=args.epochs, lr=args.lr, seed=args.seed)
     t_train = time.time() - t1
 
     pred = sel.predict(te["X"], te["feasible"])
@@ -61,7 +109,8 @@ def main(argv=None):
                    "label_counts_test": {names[k]: int(v) for k, v in
                                          sorted(collections.Counter(te["labels"].tolist()).items())},
                    "seconds": t_corpus},
-        "training": {"epochs": args.epochs, "lr": args.lr, "loss_first": hist[0], "loss_last": hist[-1],
+        "training": {"epochs": args.epochs, "lr": args.lr, "seed": args.seed, "selection": selection,
+                     "loss_first": hist[0], "loss_last": hist[-1],
                      "seconds": t_train, "train_accuracy": float(np.mean(
                          sel.predict(tr["X"], tr["feasible"]) == tr["labels"]))},
         "test": {"learned": selector.evaluate(te["times"], pred),
