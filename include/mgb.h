@@ -215,7 +215,14 @@ int mgb_dot_f64_async(int64_t n, const double* x, const double* y, double* d_res
 int mgb_dot_f32_async(int64_t n, const float* x, const float* y, float* d_result, void* stream);
 
 /* Morpheus::reduce<ExecSpace>(in, size) (core/src/Morpheus_Reduction.hpp:46-52);
- * replaces impl/DenseVector/Cuda/Morpheus_Reduction_Impl.hpp:175-234. */
+ * replaces impl/DenseVector/Cuda/Morpheus_Reduction_Impl.hpp:175-234.  The
+ * sum is deterministic for a given size and GPU.  In FP64, vectors of a few
+ * million elements or more have 7 of every 16 elements added exactly in
+ * 128-bit fixed point on the integer pipe and the rest in FP64 (the FP64
+ * add rate of this GPU would otherwise bound the sum below HBM bandwidth);
+ * the error is within that of an FP64 tree sum, and Inf / NaN propagate as
+ * in the Serial sum.  A sum whose FP64 partial sums would overflow can come
+ * out finite when the exact part carries it. */
 int mgb_reduce_f64(const double* in, int64_t size, double* result, void* stream);
 int mgb_reduce_f32(const float* in, int64_t size, float* result, void* stream);
 int mgb_reduce_f64_async(const double* in, int64_t size, double* d_result, void* stream);
