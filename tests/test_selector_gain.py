@@ -86,3 +86,17 @@ def test_learned_selector_gain_gpu_forward(cuda, corpus):
     agree = np.mean(choice == _oracle_predict(corpus["Xte"], corpus["Fte"]))
     assert agree >= 0.99, agree
     _check_gain(choice, corpus)
+
+
+def test_saved_corpus_reloads_for_training():
+    """selector_train --corpus-in reads what --corpus-out wrote: features,
+    feasibility, times and argmin labels of both parts (family names when the
+    corpus carries them)."""
+    from morpheus_gb300 import selector_train
+    tr, te = selector_train.load_corpus(CORPUS)
+    d = np.load(CORPUS)
+    assert np.array_equal(tr["X"], d["Xtr"]) and np.array_equal(te["times"], d["Tte"])
+    assert np.array_equal(tr["labels"], np.argmin(d["Ttr"], axis=1))
+    assert len(tr["desc"]) == len(tr["X"]) and len(te["desc"]) == len(te["X"])
+    # a label is always a feasible format
+    assert np.all(tr["feasible"][np.arange(len(tr["labels"])), tr["labels"]] > 0)
