@@ -239,9 +239,10 @@ int launch_rows_cfg(const mgb_csr* A, const T* x, T* y, int init, cudaStream_t s
 }
 
 // CTAs per SM of a staging configuration: as many as fit a shared-memory
-// budget (180 KB for neighbouring columns: resident warps for the
-// latency-bound tiles; 135 KB for scattered columns: L1 for the misses in
-// flight), at most 12.  Measured on GB300 (us per SpMV, FP64, TILE x CTAs):
+// budget (neighbouring columns: resident warps for the latency-bound tiles,
+// 180 KB in FP64, 215 KB in FP32 -- the 27-point stencil in FP32, 896 x 6:
+// 185.0 us, 896 x 7: 172.5 us; 135 KB for scattered columns: L1 for the
+// misses in flight), at most 12.  Measured on GB300 (us per SpMV, FP64, TILE x CTAs):
 //   5-point Laplacian 2048^2:      224 x 12  69.6
 //   band of 13, N = 2M:            448 x 10  78.5   448 x 8  71.7
 //   27-point stencil 160^3:        896 x 5  342.8   896 x 4  319.7   896 x 3  388.7
@@ -251,7 +252,7 @@ int launch_rows_cfg(const mgb_csr* A, const T* x, T* y, int init, cudaStream_t s
 template <typename T>
 constexpr int rows_ctas(int tile, bool gather) {
   const int per_cta = ROWS_WARPS * tile * (int)(sizeof(T) + sizeof(int32_t)) + 1024;
-  const int n = (gather ? 135 * 1024 : 180 * 1024) / per_cta;
+  const int n = (gather ? 135 * 1024 : (sizeof(T) == 4 ? 215 : 180) * 1024) / per_cta;
   return n > 12 ? 12 : (n < 1 ? 1 : n);
 }
 
