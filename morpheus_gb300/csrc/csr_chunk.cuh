@@ -54,30 +54,6 @@ struct XGlobal {
   const T* __restrict__ p;
   __device__ __forceinline__ T operator()(int32_t c) const { return __ldg(p + c); }
 };
-
-// read-only load that does not allocate a line in L1
-__device__ __forceinline__ double ld_nc_no_allocate(const double* p) {
-  double v;
-  asm("ld.global.nc.L1::no_allocate.f64 %0, [%1];" : "=d"(v) : "l"(p));
-  return v;
-}
-__device__ __forceinline__ float ld_nc_no_allocate(const float* p) {
-  float v;
-  asm("ld.global.nc.L1::no_allocate.f32 %0, [%1];" : "=f"(v) : "l"(p));
-  return v;
-}
-
-// x read without L1 allocation: for one matrix whose x reads are scattered
-// (about 2 % L1 hits on the power-law matrix) the lines they would allocate
-// only evict the staged stream's.  Measured (N = 2e6 power law, lane
-// segments): FP64 195.1 -> 191.4 us, FP32 165.0 -> 159.5 us.  The batched
-// kernels keep XGlobal: there the warps of an SM share a matrix's x in L1
-// (chunk queue 0.754 -> 0.770 ms without allocation).
-template <typename T>
-struct XGlobalNoAlloc {
-  const T* __restrict__ p;
-  __device__ __forceinline__ T operator()(int32_t c) const { return ld_nc_no_allocate(p + c); }
-};
 // x staged in shared memory (p points into the kernel's shared array)
 template <typename T>
 struct XShared {

@@ -67,8 +67,8 @@ spmv_csr_segments(int64_t nrows, int64_t ncols, int64_t nnz, int64_t nchunks, in
   for (int64_t wc = (int64_t)blockIdx.x * CSR_WARPS + w; wc < nchunks;
        wc += (int64_t)gridDim.x * CSR_WARPS) {
     const csr::RowRange rows = plan ? csr::planned_rows(wc, nrows, plan) : csr::chunk_rows(wc, chunk, nrows, ro, lane);
-    const csr::RowRange rr = csr::csr_rows_x<T, csr::CSR_SEG, csr::XGlobalNoAlloc<T>, true, IDX>(
-        rows, nrows, ncols, ro, ci, va, csr::XGlobalNoAlloc<T>{x}, y, init, stage[w], lane);
+    const csr::RowRange rr = csr::csr_rows_x<T, csr::CSR_SEG, csr::XGlobal<T>, true, IDX>(
+        rows, nrows, ncols, ro, ci, va, csr::XGlobal<T>{x}, y, init, stage[w], lane);
     if (DOT) {
       __syncwarp();  // the chunk's y entries, written by any lane, are visible to the warp
       for (int64_t r = rr.begin + lane; r < rr.end; r += 32) part = fmadd(x[r], y[r], part);
