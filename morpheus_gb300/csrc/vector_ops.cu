@@ -91,7 +91,9 @@ struct ExactSum {
       acc >>= min(s - S, 127);
       S = s;
     }
-    acc += ((__int128)ms << 64) >> min(S - s + EXACT_HEADROOM, 127);
+    // ms * 2^64 (the bit pattern shifted as unsigned: no signed left shift)
+    const __int128 t = (__int128)((unsigned __int128)(uint64_t)ms << 64);
+    acc += t >> min(S - s + EXACT_HEADROOM, 127);
   }
 
   // the accumulated value as a double (at most two roundings)
